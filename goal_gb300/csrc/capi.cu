@@ -1,0 +1,523 @@
+// C ABI (include/goal_gb300.h): handles over Disc, Mechanics, SolInfo and the
+// boundary conditions, with host<->device layout conversions.
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "../../include/goal_gb300.h"
+#include "capi_internal.cuh"
+
+namespace goal {
+
+std::atomic<long long> g_launches{0};
+static thread_local std::string t_last_error;
+void set_last_error(const std::string& msg) { t_last_error = msg; }
+
+namespace {
+
+__global__ void k_soa_to_orig(int E, int nc, const double* soa, const int* orig, double* out) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
+    int e = orig[s];
+    for (int q = 0; q < nc; ++q) out[(size_t)e * nc + q] = soa[(size_t)q * E + s];
+  }
+}
+__global__ void k_orig_to_soa(int E, int nc, const double* in, const int* orig, double* soa) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
+    int e = orig[s];
+    for (int q = 0; q < nc; ++q) soa[(size_t)q * E + s] = in[(size_t)e * nc + q];
+  }
+}
+__global__ void k_bsr_to_csr(int N, const int* brow_ptr, const double* A, double* csr) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    int b0 = brow_ptr[n], deg = brow_ptr[n + 1] - b0;
+    for (int k = b0; k < b0 + deg; ++k)
+      for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) csr[16ll * b0 + 4ll * r * deg + 4ll * (k - b0) + c] = A[16ll * k + 4 * r + c];
+  }
+}
+__global__ void k_colors_orig(int E, const int* color, const int* orig, int* out) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) out[orig[s]] = color[s];
+}
+
+}  // namespace
+
+void states_to_host(const Mechanics& m, int which, double* out) {
+  const Disc& d = *m.disc;
+  const int E = d.num_elems;
+  const double* src = nullptr;
+  int nc = 9;
+  switch (which) {
+    case GOAL_STATE_SIGMA: src = m.st.sigma.ptr; break;
+    case GOAL_STATE_FP: src = m.st.Fp.ptr; break;
+    case GOAL_STATE_FP_OLD: src = m.st.Fp_old.ptr; break;
+    case GOAL_STATE_EQPS: src = m.st.eqps.ptr; nc = 1; break;
+    case GOAL_STATE_EQPS_OLD: src = m.st.eqps_old.ptr; nc = 1; break;
+    default: throw Error(GOAL_ERR_ARG, "unknown state field");
+  }
+  DevBuf<double> tmp;
+  tmp.alloc((size_t)nc * E);
+  k_soa_to_orig<<<grid_for(E, 256), 256, 0, d.stream>>>(E, nc, src, d.elem_orig.ptr, tmp.ptr);
+  GOAL_CHECK_LAUNCH();
+  tmp.download(out, d.stream);
+  GOAL_CUDA(cudaStreamSynchronize(d.stream));
+}
+
+void states_from_host(Mechanics& m, int which, const double* in) {
+  const Disc& d = *m.disc;
+  const int E = d.num_elems;
+  double* dst = nullptr;
+  int nc = 9;
+  switch (which) {
+    case GOAL_STATE_SIGMA: dst = m.st.sigma.ptr; break;
+    case GOAL_STATE_FP: dst = m.st.Fp.ptr; break;
+    case GOAL_STATE_FP_OLD: dst = m.st.Fp_old.ptr; break;
+    case GOAL_STATE_EQPS: dst = m.st.eqps.ptr; nc = 1; break;
+    case GOAL_STATE_EQPS_OLD: dst = m.st.eqps_old.ptr; nc = 1; break;
+    default: throw Error(GOAL_ERR_ARG, "unknown state field");
+  }
+  DevBuf<double> tmp;
+  tmp.upload(in, (size_t)nc * E, d.stream);
+  k_orig_to_soa<<<grid_for(E, 256), 256, 0, d.stream>>>(E, nc, tmp.ptr, d.elem_orig.ptr, dst);
+  GOAL_CHECK_LAUNCH();
+  if (which == GOAL_STATE_FP_OLD) m.refresh_cpinv();
+  GOAL_CUDA(cudaStreamSynchronize(d.stream));
+}
+
+void bsr_to_csr(const SolInfo& s, double* out_host) {
+  const Disc& d = *s.disc;
+  DevBuf<double> tmp;
+  tmp.alloc(d.nnz);
+  k_bsr_to_csr<<<grid_for(d.num_nodes, 128), 128, 0, d.stream>>>(d.num_nodes, d.brow_ptr.ptr, s.A.ptr, tmp.ptr);
+  GOAL_CHECK_LAUNCH();
+  tmp.download(out_host, d.stream);
+  GOAL_CUDA(cudaStreamSynchronize(d.stream));
+}
+
+}  // namespace goal
+
+using namespace goal;
+
+struct goal_disc_s {
+  std::unique_ptr<Disc> d;
+  bool owns_stream = false;
+  ~goal_disc_s() {
+    cudaStream_t s = d ? d->stream : nullptr;
+    d.reset();
+    if (owns_stream && s) cudaStreamDestroy(s);
+  }
+};
+struct goal_mechanics_s {
+  std::unique_ptr<Mechanics> m;
+  DevBuf<double> Zd, Zc;
+};
+struct goal_sol_info_s {
+  std::unique_ptr<SolInfo> s;
+};
+struct goal_bcs_s {
+  Disc* d = nullptr;
+  std::vector<DBC> dbcs;
+  std::vector<TBC> tbcs;
+};
+
+#define GOAL_API_BEGIN try {
+#define GOAL_API_END                                      \
+  }                                                       \
+  catch (const goal::Error& e) {                          \
+    goal::set_last_error(e.what());                       \
+    return e.code;                                        \
+  }                                                       \
+  catch (const std::exception& e) {                       \
+    goal::set_last_error(e.what());                       \
+    return GOAL_ERR_STATE;                                \
+  }                                                       \
+  return GOAL_OK;
+
+#define GOAL_ARG(cond, msg) GOAL_REQUIRE(cond, GOAL_ERR_ARG, msg)
+
+extern "C" {
+
+const char* goal_last_error(void) { return t_last_error.c_str(); }
+
+long long goal_launch_count(void) { return g_launches.load(); }
+
+int goal_eval(const char* expr, double x, double y, double z, double t, double* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(expr && out, "goal_eval: null argument");
+  ExprCode c;
+  std::string err;
+  GOAL_REQUIRE(compile_expr(expr, c, err), GOAL_ERR_ARG, err);
+  *out = eval_expr(c, x, y, z, t);
+  GOAL_API_END
+}
+
+int goal_disc_create(int num_nodes, int num_elems, const double* coords, const int* tets, const int* elem_set,
+                     int num_elem_sets, goal_disc* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(out && coords && tets && num_nodes > 0 && num_elems > 0, "goal_disc_create: bad arguments");
+  GOAL_ARG(num_elem_sets >= 1, "goal_disc_create: need at least one element set");
+  for (long long i = 0; i < 4ll * num_elems; ++i)
+    GOAL_ARG(tets[i] >= 0 && tets[i] < num_nodes, "goal_disc_create: tet node out of range");
+  auto h = std::make_unique<goal_disc_s>();
+  h->d = std::make_unique<Disc>();
+  Disc& d = *h->d;
+  GOAL_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
+  h->owns_stream = true;
+  d.num_nodes = num_nodes;
+  d.num_elems = num_elems;
+  d.num_elem_sets = num_elem_sets;
+  d.coords_h.assign(coords, coords + 3ll * num_nodes);
+  d.tets_h.assign(tets, tets + 4ll * num_elems);
+  if (elem_set) {
+    d.elem_set_h.assign(elem_set, elem_set + num_elems);
+    for (int e : d.elem_set_h) GOAL_ARG(e >= 0 && e < num_elem_sets, "goal_disc_create: element set out of range");
+  } else {
+    d.elem_set_h.assign(num_elems, 0);
+  }
+  *out = h.release();
+  GOAL_API_END
+}
+
+int goal_disc_add_node_set(goal_disc d, const char* name, int n, const int* nodes) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && name && (n == 0 || nodes), "goal_disc_add_node_set: bad arguments");
+  auto ns = std::make_unique<NodeSet>();
+  ns->name = name;
+  ns->host.assign(nodes, nodes + n);
+  for (int v : ns->host) GOAL_ARG(v >= 0 && v < d->d->num_nodes, "node set: node out of range");
+  if (d->d->built) ns->dev.upload(ns->host.data(), ns->host.size(), d->d->stream);
+  d->d->node_sets[name] = std::move(ns);
+  GOAL_API_END
+}
+
+int goal_disc_add_side_set(goal_disc d, const char* name, int n, const int* tris) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && name && (n == 0 || tris) && !d->d->built, "goal_disc_add_side_set: bad arguments (add before build)");
+  auto ss = std::make_unique<SideSet>();
+  ss->name = name;
+  ss->tris.assign(tris, tris + 3ll * n);
+  for (int v : ss->tris) GOAL_ARG(v >= 0 && v < d->d->num_nodes, "side set: node out of range");
+  d->d->side_sets[name] = std::move(ss);
+  GOAL_API_END
+}
+
+int goal_disc_build_data(goal_disc d) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d, "null disc");
+  d->d->build();
+  GOAL_API_END
+}
+
+int goal_disc_sizes(goal_disc d, long long* sizes) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && sizes, "null argument");
+  const Disc& x = *d->d;
+  sizes[0] = x.num_nodes;
+  sizes[1] = x.num_elems;
+  sizes[2] = 4ll * x.num_nodes;
+  sizes[3] = x.nnz;
+  sizes[4] = x.nnzb;
+  sizes[5] = x.num_colors;
+  GOAL_API_END
+}
+
+int goal_disc_get_graph(goal_disc d, int* row_ptr, int* col_idx) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && row_ptr && col_idx && d->d->built, "goal_disc_get_graph: disc not built");
+  d->d->csr_graph(row_ptr, col_idx);
+  GOAL_API_END
+}
+
+int goal_disc_get_mesh(goal_disc d, double* coords, int* tets, int* elem_set) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d, "null disc");
+  const Disc& x = *d->d;
+  if (coords) std::memcpy(coords, x.coords_h.data(), sizeof(double) * x.coords_h.size());
+  if (tets) std::memcpy(tets, x.tets_h.data(), sizeof(int) * x.tets_h.size());
+  if (elem_set) std::memcpy(elem_set, x.elem_set_h.data(), sizeof(int) * x.elem_set_h.size());
+  GOAL_API_END
+}
+
+int goal_disc_get_colors(goal_disc d, int* colors) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && colors && d->d->built, "goal_disc_get_colors: disc not built");
+  const Disc& x = *d->d;
+  DevBuf<int> tmp;
+  tmp.alloc(x.num_elems);
+  k_colors_orig<<<grid_for(x.num_elems, 256), 256, 0, x.stream>>>(x.num_elems, x.color.ptr, x.elem_orig.ptr, tmp.ptr);
+  GOAL_CHECK_LAUNCH();
+  tmp.download(colors, x.stream);
+  GOAL_CUDA(cudaStreamSynchronize(x.stream));
+  GOAL_API_END
+}
+
+int goal_disc_stream(goal_disc d, void** stream) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && stream, "null argument");
+  *stream = (void*)d->d->stream;
+  GOAL_API_END
+}
+
+int goal_disc_destroy(goal_disc d) {
+  GOAL_API_BEGIN
+  delete d;
+  GOAL_API_END
+}
+
+int goal_nested_create(goal_disc base, goal_disc* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(base && out && base->d->built, "goal_nested_create: base not built");
+  auto h = std::make_unique<goal_disc_s>();
+  h->d = refine_uniform(*base->d);
+  h->owns_stream = false;
+  *out = h.release();
+  GOAL_API_END
+}
+
+int goal_nested_parent_edges(goal_disc nested, int* edges) {
+  GOAL_API_BEGIN
+  GOAL_ARG(nested && edges && nested->d->base_nodes > 0, "goal_nested_parent_edges: not a nested disc");
+  nested->d->parent_edges.download(edges, nested->d->stream);
+  GOAL_CUDA(cudaStreamSynchronize(nested->d->stream));
+  GOAL_API_END
+}
+
+int goal_mechanics_create(goal_disc d, int model, const double* materials, int stabilization, goal_mechanics* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && materials && out && d->d->built, "goal_mechanics_create: bad arguments (disc must be built)");
+  GOAL_ARG(model == GOAL_MODEL_NEOHOOKEAN || model == GOAL_MODEL_J2, "unknown model");
+  auto h = std::make_unique<goal_mechanics_s>();
+  h->m = std::make_unique<Mechanics>();
+  Mechanics& m = *h->m;
+  m.disc = d->d.get();
+  m.model = model;
+  m.stabilization = stabilization != 0;
+  for (int k = 0; k < m.disc->num_elem_sets; ++k) {
+    MaterialRow r{materials[5 * k], materials[5 * k + 1], materials[5 * k + 2], materials[5 * k + 3],
+                  materials[5 * k + 4]};
+    GOAL_ARG(r.E > 0 && r.nu > -1.0 && r.nu < 0.5, "material: need E > 0 and -1 < nu < 0.5");
+    if (model == GOAL_MODEL_J2) GOAL_ARG(r.Y > 0, "J2 material: need Y > 0");
+    m.mats_h.push_back(r);
+  }
+  m.init();
+  GOAL_CUDA(cudaStreamSynchronize(m.disc->stream));
+  *out = h.release();
+  GOAL_API_END
+}
+
+int goal_mechanics_set_solution(goal_mechanics m, const double* U) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && U, "null argument");
+  m->m->U.upload(U, 4ll * m->m->disc->num_nodes, m->m->disc->stream);
+  GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_mechanics_get_solution(goal_mechanics m, double* U) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && U, "null argument");
+  m->m->U.download(U, m->m->disc->stream);
+  GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_mechanics_set_weights(goal_mechanics m, const double* z_diff, const double* z_coarse) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && z_diff && z_coarse, "null argument");
+  size_t n = 4ll * m->m->disc->num_nodes;
+  m->Zd.upload(z_diff, n, m->m->disc->stream);
+  m->Zc.upload(z_coarse, n, m->m->disc->stream);
+  GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_states_set(goal_mechanics m, int which, const double* values) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && values, "null argument");
+  states_from_host(*m->m, which, values);
+  GOAL_API_END
+}
+
+int goal_states_get(goal_mechanics m, int which, double* values) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && values, "null argument");
+  states_to_host(*m->m, which, values);
+  GOAL_API_END
+}
+
+int goal_states_update(goal_mechanics m) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m, "null argument");
+  m->m->update_states();
+  GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_mechanics_destroy(goal_mechanics m) {
+  GOAL_API_BEGIN
+  delete m;
+  GOAL_API_END
+}
+
+int goal_sol_info_create(goal_disc d, goal_sol_info* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && out && d->d->built, "goal_sol_info_create: disc not built");
+  auto h = std::make_unique<goal_sol_info_s>();
+  h->s = std::make_unique<SolInfo>();
+  h->s->init(d->d.get());
+  GOAL_CUDA(cudaStreamSynchronize(d->d->stream));
+  *out = h.release();
+  GOAL_API_END
+}
+
+int goal_sol_info_zero_all(goal_sol_info s) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s, "null argument");
+  cudaStream_t st = s->s->disc->stream;
+  s->s->R.zero(st);
+  s->s->dMdu.zero(st);
+  s->s->A.zero(st);
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  GOAL_API_END
+}
+
+int goal_sol_info_get_vector(goal_sol_info s, int which, double* values) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s && values && (which == GOAL_VEC_R || which == GOAL_VEC_DMDU), "bad arguments");
+  cudaStream_t st = s->s->disc->stream;
+  (which == GOAL_VEC_R ? s->s->R : s->s->dMdu).download(values, st);
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  GOAL_API_END
+}
+
+int goal_sol_info_set_vector(goal_sol_info s, int which, const double* values) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s && values && (which == GOAL_VEC_R || which == GOAL_VEC_DMDU), "bad arguments");
+  cudaStream_t st = s->s->disc->stream;
+  DevBuf<double>& b = (which == GOAL_VEC_R ? s->s->R : s->s->dMdu);
+  b.upload(values, b.n, st);
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  GOAL_API_END
+}
+
+int goal_sol_info_get_dRdu_csr(goal_sol_info s, double* values) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s && values, "null argument");
+  bsr_to_csr(*s->s, values);
+  GOAL_API_END
+}
+
+int goal_sol_info_get_dRdu_bsr(goal_sol_info s, double* values) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s && values, "null argument");
+  cudaStream_t st = s->s->disc->stream;
+  s->s->A.download(values, st);
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  GOAL_API_END
+}
+
+int goal_sol_info_destroy(goal_sol_info s) {
+  GOAL_API_BEGIN
+  delete s;
+  GOAL_API_END
+}
+
+int goal_assemble(goal_mechanics m, goal_sol_info s, const goal_chain* chain, double* qoi_value) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && chain, "goal_assemble: null argument");
+  GOAL_ARG(!s || s->s->disc == m->m->disc, "goal_assemble: SolInfo and Mechanics belong to different discs");
+  Chain c;
+  c.mode = chain->mode;
+  c.jacobian = chain->jacobian;
+  c.save_states = chain->save_states;
+  c.qoi = chain->qoi;
+  c.rho = chain->rho;
+  c.error_chain = chain->error_chain;
+  c.overwrite = chain->overwrite;
+  GOAL_ARG(c.mode >= 0 && c.mode <= 2 && c.qoi >= 0 && c.qoi <= 2, "goal_assemble: bad chain");
+  ErrorWeights w;
+  if (c.error_chain) {
+    GOAL_ARG(m->Zd.ptr && m->Zc.ptr, "goal_assemble: error chain needs goal_mechanics_set_weights");
+    w.Zd = m->Zd.ptr;
+    w.Zc = m->Zc.ptr;
+  }
+  double q = assemble(*m->m, s ? s->s.get() : nullptr, c, &w, m->m->disc->stream);
+  if (qoi_value) *qoi_value = q;
+  GOAL_API_END
+}
+
+int goal_bcs_create(goal_disc d, goal_bcs* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && out, "null argument");
+  auto b = std::make_unique<goal_bcs_s>();
+  b->d = d->d.get();
+  *out = b.release();
+  GOAL_API_END
+}
+
+int goal_bcs_add_dirichlet(goal_bcs b, int eq, const char* node_set, const char* expr) {
+  GOAL_API_BEGIN
+  GOAL_ARG(b && node_set && expr, "null argument");
+  GOAL_ARG(eq >= 0 && eq < 3, "dirichlet bc: component must be 0, 1 or 2");
+  auto it = b->d->node_sets.find(node_set);
+  GOAL_ARG(it != b->d->node_sets.end(), std::string("unknown node set: ") + node_set);
+  DBC bc;
+  bc.eq = eq;
+  bc.set = it->second.get();
+  std::string err;
+  GOAL_REQUIRE(compile_expr(expr, bc.code, err), GOAL_ERR_ARG, err);
+  b->dbcs.push_back(bc);
+  GOAL_API_END
+}
+
+int goal_bcs_add_traction(goal_bcs b, const char* side_set, const char* tx, const char* ty, const char* tz) {
+  GOAL_API_BEGIN
+  GOAL_ARG(b && side_set && tx && ty && tz, "null argument");
+  auto it = b->d->side_sets.find(side_set);
+  GOAL_ARG(it != b->d->side_sets.end(), std::string("unknown side set: ") + side_set);
+  TBC bc;
+  bc.set = it->second.get();
+  const char* e[3] = {tx, ty, tz};
+  for (int k = 0; k < 3; ++k) {
+    std::string err;
+    GOAL_REQUIRE(compile_expr(e[k], bc.code[k], err), GOAL_ERR_ARG, err);
+  }
+  b->tbcs.push_back(bc);
+  GOAL_API_END
+}
+
+int goal_bcs_destroy(goal_bcs b) {
+  GOAL_API_BEGIN
+  delete b;
+  GOAL_API_END
+}
+
+int goal_set_resid_dbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && s && b && b->d == m->m->disc, "goal_set_resid_dbcs: bad arguments");
+  apply_dbcs(*m->m, *s->s, b->dbcs, t, false, m->m->disc->stream);
+  GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_set_jac_dbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && s && b && b->d == m->m->disc, "goal_set_jac_dbcs: bad arguments");
+  apply_dbcs(*m->m, *s->s, b->dbcs, t, true, m->m->disc->stream);
+  GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_set_tbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t, int error_weights) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && s && b && b->d == m->m->disc, "goal_set_tbcs: bad arguments");
+  const double* zd = nullptr;
+  if (error_weights) {
+    GOAL_ARG(m->Zd.ptr, "goal_set_tbcs: error weights not set");
+    zd = m->Zd.ptr;
+  }
+  apply_tbcs(*m->m, *s->s, b->tbcs, t, zd, m->m->disc->stream);
+  GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,753 @@
+// Element kernels: residual, hand-derived tangent, QoI and DWR error chain of
+// goal's stabilized mixed u-p mechanics on linear tets, one thread per element,
+// elements of one colour per launch (no two of them share a node, so the
+// scatter into the 4x4-block matrix needs no atomics and is deterministic).
+//
+// Reference chain (one integration point, src/goal_assembly.cpp:65-88):
+//   Kinematics F = I + grad u, J = det F                   src/goal_kinematics.cpp:18-25
+//   Neohookean sigma = mu J^-5/3 dev(F F^T) + k/2 (J-1/J) I  src/goal_neohookean.cpp:59-86
+//   J2 trial be = J^-2/3 F Cp^-1 F^T, s = mu dev(be), radial return with linear
+//      hardening, eqps/Fp/sigma state writes                src/goal_J2.cpp:71-156
+//   Mixed sigma_ii += p - tr(sigma)/3                       src/goal_mixed.cpp:33-46
+//   MResidual R^u_ai += P_ij dphi_a/dx_j w dv, P = J sigma F^-T   src/goal_mresidual.cpp:25-32
+//   PResidual R^p_a += (p/kappa - (J-1/J)/2) phi_a w dv     src/goal_presidual.cpp:53-59
+//   Stabilization R^p_a += tau J C^-1_ij dp/dx_i dphi_a/dx_j w dv, tau = c0 h^2/(2 mu)
+//                                                            src/goal_stabilization.cpp:59-80
+//   scatter PRIMAL (row-wise) / ADJOINT (transposed)        src/goal_displacement.cpp:177-214
+//   QoI avg disp, KS max von Mises                          src/goal_avg_disp.cpp:16-21, src/goal_ks_vm.cpp:88-98
+//   DWR weights z_diff phi_a, stabilization with z_coarse   src/goal_displacement_adjoint.cpp:37-53,
+//                                                            src/goal_pressure_adjoint.cpp:38-49,
+//                                                            src/goal_mechanics.cpp:169-218
+//
+// Tangent (replaces Sacado FAD). With G_a = grad phi_a, H = F^-T, h_a = H G_a,
+// C = Cp^-1 (identity for neo-Hookean), B = F C F^T, Ic = tr B, m_a = F C G_a,
+// q_a = m_a - Ic/3 h_a, alpha = mu J^-2/3, s = alpha dev B, the deviatoric
+// Kirchhoff stress is S = gamma s (gamma = 1 when elastic) and
+//   P G_a = S h_a + p J h_a.
+// Its derivative in direction u_bk (dF = e_k (x) G_b) is
+//   K^uu_{ai,bk} = V [ gamma alpha c_ab d_ik + h_ai X_bk + q_ai Y_bk + h_bi Z_ak ]
+//   c_ab = G_a.C G_b,  X_b = -2/3 gamma alpha m_b + pJ h_b,
+//   Y_b = -2/3 gamma alpha h_b + alpha dgamma_b,  Z_a = (gamma alpha Ic/3 - pJ) h_a,
+// and for the plastic return (X = f / (2 mubar + kh), kh = 2K/3, or kh = 0 when
+// goal's Newton loop stops after its first iterate)
+//   dgamma_b = -A1 dmubar_b - A2 dsmag_b,  dmubar_b = 2 alpha/3 q_b,
+//   dsmag_b = -2/3 smag h_b + 2 alpha/smag s m_b,
+//   A1 = 2 f kh / (c^2 smag), A2 = 2 mubar k0 / (c smag^2).
+// The pressure rows and columns:
+//   K^up_{ai,b} = V J h_ai / 4
+//   K^pu_{a,bk} = V [ h_bk (tau J w_a - (J+1/J)/8) - tau J e_ab v_k - tau J w_b h_ak ]
+//   K^pp_{ab}   = V [ 1/(16 kappa) + tau J e_ab ]
+// with v = H grad p, w_a = v.h_a, e_ab = h_a.h_b.
+#include "mechanics.cuh"
+
+namespace goal {
+
+namespace {
+
+struct ElemArgs {
+  DiscView d;
+  const double* mats;
+  const double* U;
+  const double* Fp_old;
+  const double* eqps_old;
+  const double* Cpinv;
+  double* sigma;
+  double* Fp;
+  double* eqps;
+  double* R;
+  double* A;
+  double* dMdu;
+  double* qoi_elem;
+  const double* Zd;
+  const double* Zc;
+  int* status;
+  int begin, end;
+  int stab, save, overwrite, qoi;
+  double rho, ks_max, ks_scale;
+};
+
+__device__ __forceinline__ void ld4(const double* p, double& a, double& b, double& c, double& d) {
+  double4_32a v = *reinterpret_cast<const double4_32a*>(p);
+  a = v.x; b = v.y; c = v.z; d = v.w;
+}
+__device__ __forceinline__ void st4(double* p, double a, double b, double c, double d) {
+  double4_32a v;
+  v.x = a; v.y = b; v.z = c; v.w = d;
+  *reinterpret_cast<double4_32a*>(p) = v;
+}
+__device__ __forceinline__ void acc4(double* p, bool first, double a, double b, double c, double d) {
+  if (!first) {
+    double x, y, z, w;
+    ld4(p, x, y, z, w);
+    a += x; b += y; c += z; d += w;
+  }
+  st4(p, a, b, c, d);
+}
+
+// exp(A) for a symmetric traceless 3x3 A (A = dgam N) by the power series
+// reduced with Cayley-Hamilton: A^3 = I2 A + I3 I, I2 = tr(A^2)/2, I3 = det A.
+// Returns false if the series did not settle in 80 terms.
+__device__ bool exp_traceless_sym(const double A[3][3], double out[3][3]) {
+  double A2[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A2[i][j] = A[i][0] * A[0][j] + A[i][1] * A[1][j] + A[i][2] * A[2][j];
+  double I2 = 0.5 * (A2[0][0] + A2[1][1] + A2[2][2]);
+  double I3 = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+              A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+  // term_k = A^k/k! = x I + y A + z A^2
+  double x = 0.0, y = 0.0, z = 1.0 / 2.0;  // k = 2
+  double s0 = 1.0, s1 = 1.0, s2 = 0.5;
+  bool ok = false;
+  for (int k = 2; k < 80; ++k) {
+    double nx = z * I3, ny = x + z * I2, nz = y;
+    double inv = 1.0 / (k + 1);
+    x = nx * inv; y = ny * inv; z = nz * inv;
+    s0 += x; s1 += y; s2 += z;
+    double mag = fabs(x) + fabs(y) + fabs(z);
+    if (mag < 1e-20 * (fabs(s0) + fabs(s1) + fabs(s2))) { ok = true; break; }
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) out[i][j] = s1 * A[i][j] + s2 * A2[i][j] + (i == j ? s0 : 0.0);
+  return ok;
+}
+
+template <int MODEL, int MODE, bool JAC, bool ERR>
+__global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
+  const int s = a.begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.end) return;
+  const int E = a.d.num_elems;
+
+  int v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = __ldg(a.d.tets + q * E + s);
+  double G[4][3];
+#pragma unroll
+  for (int q = 0; q < 12; ++q) G[q / 3][q % 3] = __ldg(a.d.grads + q * E + s);
+  const double V = __ldg(a.d.vol + s);
+  const int es = __ldg(a.d.elem_set + s);
+  const double kappa = __ldg(a.mats + 5 * es + 0);
+  const double mu = __ldg(a.mats + 5 * es + 1);
+  const double Kh = __ldg(a.mats + 5 * es + 2);
+  const double Yld = __ldg(a.mats + 5 * es + 3);
+  const double c0 = __ldg(a.mats + 5 * es + 4);
+
+  // gather + interpolation (Displacement/Pressure at_point)
+  double un[4][3], pn[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) ld4(a.U + 4 * v[q], un[q][0], un[q][1], un[q][2], pn[q]);
+  double F[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double t = un[0][i] * G[0][j];
+      t += un[1][i] * G[1][j];
+      t += un[2][i] * G[2][j];
+      t += un[3][i] * G[3][j];
+      F[i][j] = t;
+    }
+  double uval[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) uval[i] = ((un[0][i] * 0.25 + un[1][i] * 0.25) + un[2][i] * 0.25) + un[3][i] * 0.25;
+  F[0][0] += 1.0; F[1][1] += 1.0; F[2][2] += 1.0;
+  const double pval = ((pn[0] * 0.25 + pn[1] * 0.25) + pn[2] * 0.25) + pn[3] * 0.25;
+  double gp[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) gp[i] = ((pn[0] * G[0][i] + pn[1] * G[1][i]) + pn[2] * G[2][i]) + pn[3] * G[3][i];
+
+  // kinematics: J and H = F^-T
+  double cof[3][3];
+  cof[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+  cof[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+  cof[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+  cof[1][0] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
+  cof[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
+  cof[1][2] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
+  cof[2][0] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
+  cof[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
+  cof[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+  const double J = F[0][0] * cof[0][0] + F[0][1] * cof[0][1] + F[0][2] * cof[0][2];
+  const double Jinv = 1.0 / J;
+  double H[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) H[i][j] = cof[i][j] * Jinv;
+
+  // right Cauchy-Green of the plastic part (identity for neo-Hookean)
+  double C[6] = {1.0, 1.0, 1.0, 0.0, 0.0, 0.0};  // xx yy zz xy yz xz
+  if (MODEL == MODEL_J2) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) C[q] = __ldg(a.Cpinv + q * E + s);
+  }
+  // FC = F C
+  double FC[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    FC[i][0] = F[i][0] * C[0] + F[i][1] * C[3] + F[i][2] * C[5];
+    FC[i][1] = F[i][0] * C[3] + F[i][1] * C[1] + F[i][2] * C[4];
+    FC[i][2] = F[i][0] * C[5] + F[i][1] * C[4] + F[i][2] * C[2];
+  }
+  // B = F C F^T (symmetric)
+  double B00 = FC[0][0] * F[0][0] + FC[0][1] * F[0][1] + FC[0][2] * F[0][2];
+  double B11 = FC[1][0] * F[1][0] + FC[1][1] * F[1][1] + FC[1][2] * F[1][2];
+  double B22 = FC[2][0] * F[2][0] + FC[2][1] * F[2][1] + FC[2][2] * F[2][2];
+  double B01 = FC[0][0] * F[1][0] + FC[0][1] * F[1][1] + FC[0][2] * F[1][2];
+  double B12 = FC[1][0] * F[2][0] + FC[1][1] * F[2][1] + FC[1][2] * F[2][2];
+  double B02 = FC[0][0] * F[2][0] + FC[0][1] * F[2][1] + FC[0][2] * F[2][2];
+  const double Ic = B00 + B11 + B22;
+  const double Jm13 = rcbrt(J);
+  const double alpha = mu * (Jm13 * Jm13);
+  const double Ic3 = Ic / 3.0;
+  // trial deviatoric Kirchhoff stress s = alpha dev(B)
+  const double s00 = alpha * (B00 - Ic3), s11 = alpha * (B11 - Ic3), s22 = alpha * (B22 - Ic3);
+  const double s01 = alpha * B01, s12 = alpha * B12, s02 = alpha * B02;
+
+  // J2 radial return (closed form of goal's scalar Newton loop)
+  double gamma = 1.0;
+  bool plastic = false;
+  double smag = 0.0, mubar = 0.0, fyield = 0.0, k0 = 0.0, cc = 1.0, kh = 0.0, Xr = 0.0;
+  const double sq23 = 0.81649658092772603273;  // sqrt(2/3)
+  if (MODEL == MODEL_J2 || (a.qoi == QOI_KS_VM)) {
+    smag = sqrt(s00 * s00 + s11 * s11 + s22 * s22 + 2.0 * (s01 * s01 + s12 * s12 + s02 * s02));
+  }
+  if (MODEL == MODEL_J2) {
+    mubar = alpha * Ic3;
+    const double eq_old = __ldg(a.eqps_old + s);
+    k0 = sq23 * (Yld + Kh * eq_old);
+    fyield = smag - k0;
+    if (fyield > 1.0e-12) {
+      plastic = true;
+      // first Newton iterate of src/goal_J2.cpp:101-121 (H = 0 in the first slope)
+      double X1 = -(fyield / (-2.0 * mubar * 1.0));
+      double alpha1 = eq_old + sq23 * X1;
+      double R1 = smag - (2.0 * mubar * X1 + sq23 * (Yld + Kh * alpha1));
+      double r1 = fabs(R1);
+      bool conv1 = (r1 < 1.0e-11) || (r1 / Yld < 1.0e-11) || (r1 / fyield < 1.0e-11);
+      kh = conv1 ? 0.0 : (2.0 / 3.0) * Kh;
+      cc = 2.0 * mubar + kh;
+      Xr = conv1 ? X1 : fyield / cc;
+      gamma = 1.0 - 2.0 * mubar * Xr / smag;
+      if (!(Xr >= 0.0) || !isfinite(Xr)) atomicOr(a.status, 1);
+      if (a.save) {
+        a.eqps[s] = eq_old + sq23 * Xr;
+        // Fp = exp(dgam N) Fp_old (stored only at plastic points)
+        const double is = Xr / smag;
+        const double Am[3][3] = {{s00 * is, s01 * is, s02 * is}, {s01 * is, s11 * is, s12 * is},
+                                 {s02 * is, s12 * is, s22 * is}};
+        double Ex[3][3];
+        if (!exp_traceless_sym(Am, Ex)) atomicOr(a.status, 2);
+        double Fo[3][3];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) Fo[q / 3][q % 3] = __ldg(a.Fp_old + q * E + s);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            a.Fp[(3 * i + j) * E + s] = Ex[i][0] * Fo[0][j] + Ex[i][1] * Fo[1][j] + Ex[i][2] * Fo[2][j];
+      }
+    } else if (a.save) {
+      a.eqps[s] = eq_old;
+    }
+  }
+
+  // Cauchy stress of the model, then Mixed
+  const double pm = 0.5 * kappa * (J - Jinv);
+  const double gJ = gamma * Jinv;
+  double sg[3][3];
+  sg[0][0] = s00 * gJ + pm; sg[1][1] = s11 * gJ + pm; sg[2][2] = s22 * gJ + pm;
+  sg[0][1] = sg[1][0] = s01 * gJ;
+  sg[1][2] = sg[2][1] = s12 * gJ;
+  sg[0][2] = sg[2][0] = s02 * gJ;
+  {
+    double pbar = ((sg[0][0] + sg[1][1]) + sg[2][2]) / 3.0;
+    double dp = pval - pbar;
+    sg[0][0] += dp; sg[1][1] += dp; sg[2][2] += dp;
+  }
+  if (a.save) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) a.sigma[q * E + s] = sg[q / 3][q % 3];
+  }
+
+  // h_a = H G_a
+  double hv[4][3];
+#pragma unroll
+  for (int n = 0; n < 4; ++n)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) hv[n][i] = H[i][0] * G[n][0] + H[i][1] * G[n][1] + H[i][2] * G[n][2];
+  // v = H grad p, w_a = v.h_a
+  double vv[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) vv[i] = H[i][0] * gp[0] + H[i][1] * gp[1] + H[i][2] * gp[2];
+  double wv[4];
+#pragma unroll
+  for (int n = 0; n < 4; ++n) wv[n] = vv[0] * hv[n][0] + vv[1] * hv[n][1] + vv[2] * hv[n][2];
+  double tau = 0.0;
+  if (a.stab) {
+    const double hh = __ldg(a.d.h + s);
+    tau = 0.5 * c0 * hh * hh / mu;
+  }
+  const double tauJ = tau * J;
+  const double dUdJ = 0.5 * (J - Jinv);
+  double T[3][3];  // J sigma
+#pragma unroll
+  for (int q = 0; q < 9; ++q) T[q / 3][q % 3] = J * sg[q / 3][q % 3];
+
+  // ---------------------------------------------------------------- residual
+  if (MODE != MODE_NONE) {
+    double Ru[4][3], Rp[4];
+    if (!ERR) {
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Ru[n][i] = V * (T[i][0] * hv[n][0] + T[i][1] * hv[n][1] + T[i][2] * hv[n][2]);
+        Rp[n] = ((pval / kappa) - dUdJ) * 0.25 * V + (a.stab ? tauJ * wv[n] * V : 0.0);
+      }
+    } else {
+      // DWR weights: z_diff phi_a (momentum, pressure), z_coarse phi_a (stabilization)
+      double zn[4][4], zcn[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        ld4(a.Zd + 4 * v[q], zn[q][0], zn[q][1], zn[q][2], zn[q][3]);
+        zcn[q] = __ldg(a.Zc + 4 * v[q] + 3);
+      }
+      double z[3], gz[3][3], zp, zc, gzc[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        z[i] = 0.25 * (zn[0][i] + zn[1][i] + zn[2][i] + zn[3][i]);
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          gz[i][j] = zn[0][i] * G[0][j] + zn[1][i] * G[1][j] + zn[2][i] * G[2][j] + zn[3][i] * G[3][j];
+      }
+      zp = 0.25 * (zn[0][3] + zn[1][3] + zn[2][3] + zn[3][3]);
+      zc = 0.25 * (zcn[0] + zcn[1] + zcn[2] + zcn[3]);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) gzc[j] = zcn[0] * G[0][j] + zcn[1] * G[1][j] + zcn[2] * G[2][j] + zcn[3] * G[3][j];
+      double P[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) P[i][j] = T[i][0] * H[0][j] + T[i][1] * H[1][j] + T[i][2] * H[2][j];
+      double Pg[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Pg[i] = P[i][0] * gz[i][0] + P[i][1] * gz[i][1] + P[i][2] * gz[i][2];
+      double hz[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) hz[i] = H[i][0] * gzc[0] + H[i][1] * gzc[1] + H[i][2] * gzc[2];
+      const double vhz = vv[0] * hz[0] + vv[1] * hz[1] + vv[2] * hz[2];
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          double PGa = T[i][0] * hv[n][0] + T[i][1] * hv[n][1] + T[i][2] * hv[n][2];
+          Ru[n][i] = V * (0.25 * Pg[i] + z[i] * PGa);
+        }
+        Rp[n] = ((pval / kappa) - dUdJ) * (zp * 0.25) * V + (a.stab ? tauJ * (0.25 * vhz + zc * wv[n]) * V : 0.0);
+      }
+    }
+    const unsigned fm = a.overwrite ? __ldg(a.d.first + s) : 0u;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) acc4(a.R + 4 * v[n], (fm >> (16 + n)) & 1u, Ru[n][0], Ru[n][1], Ru[n][2], Rp[n]);
+  }
+
+  // ---------------------------------------------------------------- QoI
+  double ks_w = 0.0;
+  if (a.qoi == QOI_AVG_DISP) {
+    double ev = 0.0;
+    ev += uval[0] * V;
+    ev += uval[1] * V;
+    ev += uval[2] * V;
+    a.qoi_elem[s] = ev / 3.0;
+  } else if (a.qoi == QOI_KS_VM) {
+    double d1 = sg[0][0] - sg[1][1], d2 = sg[1][1] - sg[2][2], d3 = sg[2][2] - sg[0][0];
+    double s7 = 0.5 * (d1 * d1 + d2 * d2 + d3 * d3 + 6.0 * (sg[0][1] * sg[0][1] + sg[1][2] * sg[1][2] + sg[2][0] * sg[2][0]));
+    double vm = sqrt(s7);
+    double ex = exp(a.rho * (vm - a.ks_max));
+    a.qoi_elem[s] = (1.0 / (a.rho * a.ks_scale)) * ex * V;
+    ks_w = (V / a.ks_scale) * ex;  // d(elem value)/d(vm)
+  }
+
+  if constexpr (JAC) {
+  // ---------------------------------------------------------------- tangent
+  // m_a = F C G_a, q_a = m_a - Ic/3 h_a
+  double mv[4][3], qv[4][3];
+#pragma unroll
+  for (int n = 0; n < 4; ++n)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      mv[n][i] = FC[i][0] * G[n][0] + FC[i][1] * G[n][1] + FC[i][2] * G[n][2];
+      qv[n][i] = mv[n][i] - Ic3 * hv[n][i];
+    }
+  const double pJ = pval * J;
+  const double ga = gamma * alpha;
+  // dgamma_b = yq q_b + yh h_b + yn (s m_b) ; Y_b = -2/3 ga h_b + alpha dgamma_b
+  double yq = 0.0, yh = 0.0, yn = 0.0;
+  // d(gamma smag) = dq q_b + dh h_b + dn (s m_b)   (KS derivative)
+  double vq = 0.0, vh = 0.0, vn = 0.0;
+  const bool need_n = plastic || (a.qoi == QOI_KS_VM);
+  if (plastic) {
+    const double A1 = 2.0 * fyield * kh / (cc * cc * smag);
+    const double A2 = 2.0 * mubar * k0 / (cc * smag * smag);
+    yq = -A1 * (2.0 * alpha / 3.0);
+    yh = A2 * (2.0 / 3.0) * smag;
+    yn = -A2 * (2.0 * alpha / smag);
+  }
+  if (a.qoi == QOI_KS_VM) {
+    // dsmag_b = -2/3 smag h_b + 2 alpha/smag n_b ; dmubar_b = 2 alpha/3 q_b
+    double fs = 1.0, fmu = 0.0;
+    if (plastic) { fs = kh / cc; fmu = -2.0 * fyield * kh / (cc * cc); }
+    vh = fs * (-(2.0 / 3.0) * smag);
+    vn = fs * (2.0 * alpha / smag);
+    vq = fmu * (2.0 * alpha / 3.0);
+  }
+  double Xp[4][3], Yp[4][3], nv[4][3];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    if (need_n) {
+      nv[b][0] = s00 * mv[b][0] + s01 * mv[b][1] + s02 * mv[b][2];
+      nv[b][1] = s01 * mv[b][0] + s11 * mv[b][1] + s12 * mv[b][2];
+      nv[b][2] = s02 * mv[b][0] + s12 * mv[b][1] + s22 * mv[b][2];
+    } else {
+      nv[b][0] = nv[b][1] = nv[b][2] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      Xp[b][k] = V * (-(2.0 / 3.0) * ga * mv[b][k] + pJ * hv[b][k]);
+      Yp[b][k] = V * (-(2.0 / 3.0) * ga * hv[b][k] + alpha * (yq * qv[b][k] + yh * hv[b][k] + yn * nv[b][k]));
+    }
+  }
+  // dM/du (QoI derivative) for the u dofs; pressure dofs do not enter the QoIs
+  if (a.qoi != QOI_NONE) {
+    const unsigned fm = a.overwrite ? __ldg(a.d.first + s) : 0u;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      double d[3];
+      if (a.qoi == QOI_AVG_DISP) {
+        d[0] = d[1] = d[2] = V / 12.0;
+      } else {
+        const double c1 = ks_w * 1.22474487139158904909 * Jinv;  // sqrt(3/2)/J
+        const double gs = gamma * smag;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          d[k] = c1 * (vq * qv[b][k] + vh * hv[b][k] + vn * nv[b][k] - gs * hv[b][k]);
+      }
+      acc4(a.dMdu + 4 * v[b], (fm >> (16 + b)) & 1u, d[0], d[1], d[2], 0.0);
+    }
+  }
+
+  const double zs = V * (ga * Ic3 - pJ);
+  const double gaV = ga * V;
+  const double upf = V * J * 0.25;
+  const double tJV = tauJ * V;
+  const double ppc = V / (16.0 * kappa);
+  const double pu0 = V * ((J + Jinv) * 0.125);
+  const unsigned fm = a.overwrite ? __ldg(a.d.first + s) : 0u;
+#pragma unroll
+  for (int ai = 0; ai < 4; ++ai) {
+    double CG[3];  // C G_a
+    CG[0] = C[0] * G[ai][0] + C[3] * G[ai][1] + C[5] * G[ai][2];
+    CG[1] = C[3] * G[ai][0] + C[1] * G[ai][1] + C[4] * G[ai][2];
+    CG[2] = C[5] * G[ai][0] + C[4] * G[ai][1] + C[2] * G[ai][2];
+    const double Za0 = zs * hv[ai][0], Za1 = zs * hv[ai][1], Za2 = zs * hv[ai][2];
+    const double pu1 = (a.stab ? tJV * wv[ai] : 0.0) - pu0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const double cab = gaV * (CG[0] * G[b][0] + CG[1] * G[b][1] + CG[2] * G[b][2]);
+      const double eab = hv[ai][0] * hv[b][0] + hv[ai][1] * hv[b][1] + hv[ai][2] * hv[b][2];
+      double K[4][4];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const double Zak = (k == 0) ? Za0 : ((k == 1) ? Za1 : Za2);
+          double t = hv[ai][i] * Xp[b][k] + qv[ai][i] * Yp[b][k] + hv[b][i] * Zak;
+          if (i == k) t += cab;
+          K[i][k] = t;
+        }
+        K[i][3] = upf * hv[ai][i];
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double t = pu1 * hv[b][k];
+        if (a.stab) t -= tJV * (eab * vv[k] + wv[b] * hv[ai][k]);
+        K[3][k] = t;
+      }
+      K[3][3] = ppc + (a.stab ? tJV * eab : 0.0);
+      if (MODE == MODE_PRIMAL) {
+        const int q = 4 * ai + b;
+        double* blk = a.A + 16ll * __ldg(a.d.blk + q * E + s);
+        const bool f1 = (fm >> q) & 1u;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc4(blk + 4 * r, f1, K[r][0], K[r][1], K[r][2], K[r][3]);
+      } else if (MODE == MODE_ADJOINT) {
+        const int q = 4 * b + ai;
+        double* blk = a.A + 16ll * __ldg(a.d.blk + q * E + s);
+        const bool f1 = (fm >> q) & 1u;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc4(blk + 4 * r, f1, K[0][r], K[1][r], K[2][r], K[3][r]);
+      }
+    }
+  }
+  }  // JAC
+}
+
+// ------------------------------------------------------------------ reductions
+__global__ void k_sum_partial(const double* x, int n, double* part) {
+  KSum acc;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc.add(x[i]);
+  acc = block_reduce(acc);
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = acc.s; part[2 * blockIdx.x + 1] = acc.c; }
+}
+__global__ void k_sum_final(const double* part, int nb, double* out) {
+  KSum acc;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    KSum t;
+    t.s = part[2 * i];
+    t.c = part[2 * i + 1];
+    acc.add(t);
+  }
+  acc = block_reduce(acc);
+  if (threadIdx.x == 0) out[0] = acc.value();
+}
+
+__device__ __forceinline__ double vm_of(const double* sig, int E, int s) {
+  double a00 = sig[0 * E + s], a11 = sig[4 * E + s], a22 = sig[8 * E + s];
+  double a01 = sig[1 * E + s], a12 = sig[5 * E + s], a20 = sig[6 * E + s];
+  double d1 = a00 - a11, d2 = a11 - a22, d3 = a22 - a00;
+  return sqrt(0.5 * (d1 * d1 + d2 * d2 + d3 * d3 + 6.0 * (a01 * a01 + a12 * a12 + a20 * a20)));
+}
+
+__global__ void k_vm_max_partial(const double* sig, int E, double* part) {
+  double m = 0.0;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) m = fmax(m, vm_of(sig, E, s));
+  m = block_max(m);
+  if (threadIdx.x == 0) part[blockIdx.x] = m;
+}
+__global__ void k_max_final(const double* part, int nb, double* out) {
+  double m = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) m = fmax(m, part[i]);
+  m = block_max(m);
+  if (threadIdx.x == 0) out[0] = m;
+}
+__global__ void k_ks_terms(const double* sig, const double* vol, int E, double rho, const double* mx, double* out) {
+  double m = mx[0];
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x)
+    out[s] = exp(rho * (vm_of(sig, E, s) - m)) * vol[s];
+}
+
+__global__ void k_cpinv(int E, const double* Fp_old, double* Cpinv) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
+    double A[3][3];
+    for (int q = 0; q < 9; ++q) A[q / 3][q % 3] = Fp_old[q * E + s];
+    double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+    double c01 = A[1][0] * A[2][2] - A[1][2] * A[2][0];
+    double c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+    double d = A[0][0] * c00 - A[0][1] * c01 + A[0][2] * c02;
+    double I[3][3];
+    I[0][0] = c00 / d;
+    I[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) / d;
+    I[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) / d;
+    I[1][0] = (A[1][2] * A[2][0] - A[1][0] * A[2][2]) / d;
+    I[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) / d;
+    I[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) / d;
+    I[2][0] = (A[1][0] * A[2][1] - A[1][1] * A[2][0]) / d;
+    I[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) / d;
+    I[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) / d;
+    // Cp^-1 = Fp^-1 Fp^-T
+    auto cc = [&](int i, int j) { return I[i][0] * I[j][0] + I[i][1] * I[j][1] + I[i][2] * I[j][2]; };
+    Cpinv[0 * E + s] = cc(0, 0);
+    Cpinv[1 * E + s] = cc(1, 1);
+    Cpinv[2 * E + s] = cc(2, 2);
+    Cpinv[3 * E + s] = cc(0, 1);
+    Cpinv[4 * E + s] = cc(1, 2);
+    Cpinv[5 * E + s] = cc(0, 2);
+  }
+}
+
+__global__ void k_fill_identity(int E, double* Fp) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x)
+    for (int q = 0; q < 9; ++q) Fp[q * E + s] = (q % 4 == 0) ? 1.0 : 0.0;
+}
+
+template <int MODEL, int MODE, bool JAC, bool ERR>
+void launch_colours(const Disc& d, ElemArgs args, cudaStream_t st) {
+  const int block = 128;
+  if constexpr (MODE == MODE_NONE) {
+    args.begin = 0;
+    args.end = d.num_elems;
+    k_elem<MODEL, MODE, JAC, ERR><<<(d.num_elems + block - 1) / block, block, 0, st>>>(args);
+    GOAL_CHECK_LAUNCH();
+  } else {
+  for (int c = 0; c < d.num_colors; ++c) {
+    args.begin = d.color_ptr[c];
+    args.end = d.color_ptr[c + 1];
+    int n = args.end - args.begin;
+    if (n <= 0) continue;
+    k_elem<MODEL, MODE, JAC, ERR><<<(n + block - 1) / block, block, 0, st>>>(args);
+    GOAL_CHECK_LAUNCH();
+  }
+  }
+}
+
+template <int MODEL>
+void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t st) {
+  if (c.error_chain) {
+    GOAL_REQUIRE(!c.jacobian && c.mode == MODE_PRIMAL, GOAL_ERR_ARG, "the error chain is a residual (PRIMAL) chain");
+    launch_colours<MODEL, MODE_PRIMAL, false, true>(d, args, st);
+    return;
+  }
+  if (c.mode == MODE_NONE) {
+    if (c.jacobian) launch_colours<MODEL, MODE_NONE, true, false>(d, args, st);
+    else launch_colours<MODEL, MODE_NONE, false, false>(d, args, st);
+  } else if (c.mode == MODE_PRIMAL) {
+    if (c.jacobian) launch_colours<MODEL, MODE_PRIMAL, true, false>(d, args, st);
+    else launch_colours<MODEL, MODE_PRIMAL, false, false>(d, args, st);
+  } else {
+    GOAL_REQUIRE(c.jacobian, GOAL_ERR_ARG, "ADJOINT mode is a Jacobian (FADT) chain");
+    launch_colours<MODEL, MODE_ADJOINT, true, false>(d, args, st);
+  }
+}
+
+double device_sum(const double* x, int n, DevBuf<double>& red, cudaStream_t st) {
+  const int nb = std::min(grid_for(n, 256), 1024);
+  if (red.n < 2 * (size_t)nb + 2) red.alloc(2 * nb + 2);
+  k_sum_partial<<<nb, 256, 0, st>>>(x, n, red.ptr);
+  GOAL_CHECK_LAUNCH();
+  k_sum_final<<<1, 1024, 0, st>>>(red.ptr, nb, red.ptr + 2 * nb);
+  GOAL_CHECK_LAUNCH();
+  double out = 0.0;
+  GOAL_CUDA(cudaMemcpyAsync(&out, red.ptr + 2 * nb, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  return out;
+}
+
+}  // namespace
+
+void Mechanics::init() {
+  const int E = disc->num_elems, N = disc->num_nodes;
+  std::vector<double> m;
+  for (const MaterialRow& r : mats_h) {
+    double kappa = r.E / (3.0 * (1.0 - 2.0 * r.nu));
+    double mu = r.E / (2.0 * (1.0 + r.nu));
+    m.insert(m.end(), {kappa, mu, r.K, r.Y, r.c0});
+  }
+  mats.upload(m.data(), m.size(), disc->stream);
+  U.alloc(4ll * N);
+  U.zero(disc->stream);
+  st.sigma.alloc(9ll * E);
+  st.sigma.zero(disc->stream);
+  st.eqps.alloc(E);
+  st.eqps.zero(disc->stream);
+  st.eqps_old.alloc(E);
+  st.eqps_old.zero(disc->stream);
+  st.Fp.alloc(9ll * E);
+  st.Fp_old.alloc(9ll * E);
+  st.Cpinv.alloc(6ll * E);
+  k_fill_identity<<<grid_for(E, 256), 256, 0, disc->stream>>>(E, st.Fp.ptr);
+  k_fill_identity<<<grid_for(E, 256), 256, 0, disc->stream>>>(E, st.Fp_old.ptr);
+  GOAL_CHECK_LAUNCH();
+  refresh_cpinv();
+  qoi_elem.alloc(E);
+  status.alloc(1);
+  status.zero(disc->stream);
+}
+
+void Mechanics::refresh_cpinv() {
+  const int E = disc->num_elems;
+  k_cpinv<<<grid_for(E, 256), 256, 0, disc->stream>>>(E, st.Fp_old.ptr, st.Cpinv.ptr);
+  GOAL_CHECK_LAUNCH();
+}
+
+void Mechanics::update_states() {
+  const int E = disc->num_elems;
+  GOAL_CUDA(cudaMemcpyAsync(st.Fp_old.ptr, st.Fp.ptr, sizeof(double) * 9 * E, cudaMemcpyDeviceToDevice, disc->stream));
+  GOAL_CUDA(cudaMemcpyAsync(st.eqps_old.ptr, st.eqps.ptr, sizeof(double) * E, cudaMemcpyDeviceToDevice, disc->stream));
+  refresh_cpinv();
+}
+
+void SolInfo::init(Disc* d) {
+  disc = d;
+  R.alloc(4ll * d->num_nodes);
+  dMdu.alloc(4ll * d->num_nodes);
+  A.alloc(16ll * d->nnzb);
+  R.zero(d->stream);
+  dMdu.zero(d->stream);
+  A.zero(d->stream);
+}
+
+void ks_prepass(Mechanics& m, double rho, double& max_vm, double& scale, cudaStream_t st) {
+  const int E = m.disc->num_elems;
+  const int nb = std::min(grid_for(E, 256), 1024);
+  if (m.red.n < 2 * (size_t)nb + 2) m.red.alloc(2 * nb + 2);
+  k_vm_max_partial<<<nb, 256, 0, st>>>(m.st.sigma.ptr, E, m.red.ptr);
+  GOAL_CHECK_LAUNCH();
+  k_max_final<<<1, 1024, 0, st>>>(m.red.ptr, nb, m.red.ptr + 2 * nb);
+  GOAL_CHECK_LAUNCH();
+  k_ks_terms<<<grid_for(E, 256), 256, 0, st>>>(m.st.sigma.ptr, m.disc->vol.ptr, E, rho, m.red.ptr + 2 * nb,
+                                               m.qoi_elem.ptr);
+  GOAL_CHECK_LAUNCH();
+  GOAL_CUDA(cudaMemcpyAsync(&max_vm, m.red.ptr + 2 * nb, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  scale = device_sum(m.qoi_elem.ptr, E, m.red, st);
+}
+
+double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w, cudaStream_t st) {
+  const Disc& d = *m.disc;
+  ElemArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.d = d.view();
+  a.mats = m.mats.ptr;
+  a.U = m.U.ptr;
+  a.Fp_old = m.st.Fp_old.ptr;
+  a.eqps_old = m.st.eqps_old.ptr;
+  a.Cpinv = m.st.Cpinv.ptr;
+  a.sigma = m.st.sigma.ptr;
+  a.Fp = m.st.Fp.ptr;
+  a.eqps = m.st.eqps.ptr;
+  a.status = m.status.ptr;
+  a.stab = m.stabilization ? 1 : 0;
+  a.save = c.save_states;
+  a.overwrite = c.overwrite;
+  a.qoi = c.qoi;
+  a.rho = c.rho;
+  a.qoi_elem = m.qoi_elem.ptr;
+  if (c.mode != MODE_NONE || c.jacobian) {
+    GOAL_REQUIRE(s != nullptr, GOAL_ERR_ARG, "assemble: SolInfo required for this chain");
+    a.R = s->R.ptr;
+    a.A = s->A.ptr;
+    a.dMdu = s->dMdu.ptr;
+  }
+  if (c.error_chain) {
+    GOAL_REQUIRE(w && w->Zd && w->Zc, GOAL_ERR_ARG, "error chain needs z weights");
+    a.Zd = w->Zd;
+    a.Zc = w->Zc;
+  }
+  double ks_max = 0.0, ks_scale = 1.0;
+  if (c.qoi == QOI_KS_VM) {
+    GOAL_REQUIRE(c.rho > 0.0, GOAL_ERR_ARG, "KS functional needs rho > 0");
+    ks_prepass(m, c.rho, ks_max, ks_scale, st);
+    GOAL_REQUIRE(ks_max > 0.0 && ks_scale > 0.0, GOAL_ERR_STATE, "KS functional: stored stresses are zero");
+  }
+  a.ks_max = ks_max;
+  a.ks_scale = ks_scale;
+  GOAL_CUDA(cudaMemsetAsync(m.status.ptr, 0, sizeof(int), st));
+  if (c.overwrite && c.jacobian && c.qoi == QOI_NONE && s) {
+    // dMdu is not written by a chain without QoI: SolInfo::zero_all semantics
+    GOAL_CUDA(cudaMemsetAsync(s->dMdu.ptr, 0, sizeof(double) * s->dMdu.n, st));
+  }
+  if (m.model == MODEL_J2) dispatch<MODEL_J2>(d, c, a, st);
+  else dispatch<MODEL_NEOHOOKEAN>(d, c, a, st);
+  int hstat = 0;
+  GOAL_CUDA(cudaMemcpyAsync(&hstat, m.status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  double q = 0.0;
+  if (c.qoi != QOI_NONE) {
+    q = device_sum(m.qoi_elem.ptr, d.num_elems, m.red, st);
+    if (c.qoi == QOI_KS_VM) q = ks_max + (1.0 / c.rho) * std::log(ks_scale);
+  } else {
+    GOAL_CUDA(cudaStreamSynchronize(st));
+  }
+  GOAL_REQUIRE(hstat == 0, GOAL_ERR_RETURN_MAP, "J2: return mapping failed");
+  return q;
+}
+
+}  // namespace goal

@@ -1,0 +1,170 @@
+/*
+ * goal_gb300.h -- C ABI of the GB300 implementation of goal's element hot path
+ * and its primal/adjoint solves.
+ *
+ * Plain pointers and sizes only. Every function returns 0 on success or a
+ * nonzero status; goal_last_error() returns the message of the last failure
+ * on the calling thread (the reference aborts through goal::fail,
+ * src/goal_control.cpp:91-99). Handles are not thread-safe; each discretization
+ * owns one CUDA stream that its mechanics, linear objects and solves use.
+ *
+ * Host arrays use goal's layouts: nodal DOF vectors are node-major with
+ * num_eqs = 4 entries per node (u_x, u_y, u_z, p; lid = node*4 + eq,
+ * src/goal_disc.cpp:195-201); element arrays are in the caller's element
+ * order; tensors are row-major 3x3.
+ */
+#ifndef GOAL_GB300_H
+#define GOAL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GOAL_OK 0
+#define GOAL_ERR_ARG 1
+#define GOAL_ERR_CUDA 2
+#define GOAL_ERR_STATE 3
+#define GOAL_ERR_RETURN_MAP 4
+#define GOAL_ERR_NEWTON 5
+#define GOAL_ERR_CAPACITY 6
+#define GOAL_ERR_SOLVER 7
+
+/* goal::EvalModes (src/goal_eval_modes.hpp:6) */
+#define GOAL_NONE 0
+#define GOAL_PRIMAL 1
+#define GOAL_ADJOINT 2
+
+/* Mechanics "model" (src/goal_mechanics.cpp:113-120) */
+#define GOAL_MODEL_NEOHOOKEAN 0
+#define GOAL_MODEL_J2 1
+
+/* functional "type" (src/goal_mechanics.cpp:148-167) */
+#define GOAL_QOI_NONE 0
+#define GOAL_QOI_AVG_DISP 1
+#define GOAL_QOI_KS_VM 2 /* "max vm" with parameter rho */
+
+/* state fields (src/goal_mechanics.cpp:87-95) */
+#define GOAL_STATE_SIGMA 0
+#define GOAL_STATE_FP 1
+#define GOAL_STATE_FP_OLD 2
+#define GOAL_STATE_EQPS 3
+#define GOAL_STATE_EQPS_OLD 4
+
+/* SolInfo vectors (src/goal_sol_info.hpp:12-16) */
+#define GOAL_VEC_R 0
+#define GOAL_VEC_DMDU 1
+
+typedef struct goal_disc_s* goal_disc;
+typedef struct goal_mechanics_s* goal_mechanics;
+typedef struct goal_sol_info_s* goal_sol_info;
+typedef struct goal_bcs_s* goal_bcs;
+
+const char* goal_last_error(void);
+
+/* Number of kernels this library has launched in the process. */
+long long goal_launch_count(void);
+
+/* goal::eval (src/goal_control.cpp:107-123): evaluates a boundary-condition
+ * expression in x, y, z, t on the host with the same program the device runs. */
+int goal_eval(const char* expr, double x, double y, double z, double t, double* out);
+
+/* ---------------------------------------------------------------- Disc
+ * goal::create_disc / Disc::build_data (src/goal_disc.hpp:95, :58;
+ * src/goal_disc.cpp:224-235). tets are positively oriented linear tets.
+ * build_data builds the node graph, the element colouring and the per-element
+ * geometry on the GPU. */
+int goal_disc_create(int num_nodes, int num_elems, const double* coords, const int* tets, const int* elem_set,
+                     int num_elem_sets, goal_disc* out);
+int goal_disc_add_node_set(goal_disc d, const char* name, int num_nodes, const int* nodes);
+int goal_disc_add_side_set(goal_disc d, const char* name, int num_sides, const int* tris);
+int goal_disc_build_data(goal_disc d);
+/* sizes[0..5] = num_nodes, num_elems, num_dofs, nnz, nnzb (4x4 blocks), num_colors */
+int goal_disc_sizes(goal_disc d, long long* sizes);
+/* The owned CSR graph of dRdu (Disc::compute_graphs, src/goal_disc.cpp:307-332):
+ * row_ptr[num_dofs+1], col_idx[nnz], columns sorted. */
+int goal_disc_get_graph(goal_disc d, int* row_ptr, int* col_idx);
+/* the mesh as stored (coords[3*num_nodes], tets[4*num_elems], elem_set[num_elems]);
+ * for a nested discretization this is the refined mesh */
+int goal_disc_get_mesh(goal_disc d, double* coords, int* tets, int* elem_set);
+/* colour of every element (caller's element order) */
+int goal_disc_get_colors(goal_disc d, int* colors);
+/* cudaStream_t of the discretization (as void*) */
+int goal_disc_stream(goal_disc d, void** stream);
+int goal_disc_destroy(goal_disc d);
+
+/* Nested(d, UNIFORM) (src/goal_nested.cpp:13-28, 144-154): uniformly refined
+ * copy of a built discretization, built. New node num_nodes(base)+k sits at the
+ * midpoint of edge k; edges are the upper triangle of the node graph in (i, j)
+ * order. Children of base element e are 8e..8e+7. */
+int goal_nested_create(goal_disc base, goal_disc* out);
+/* end points of the edge of every new node: edges[2*(n - base_nodes) + {0,1}] */
+int goal_nested_parent_edges(goal_disc nested, int* edges);
+
+/* ---------------------------------------------------------------- Mechanics
+ * goal::create_mechanics (src/goal_mechanics.hpp:50). materials holds, per
+ * element set, E, nu, K, Y, c0 (K and Y are read by J2 only). States start as
+ * sigma = 0, Fp = Fp_old = I, eqps = eqps_old = 0 (src/goal_states.cpp:99-128). */
+int goal_mechanics_create(goal_disc d, int model, const double* materials, int stabilization, goal_mechanics* out);
+int goal_mechanics_set_solution(goal_mechanics m, const double* U);  /* 4*num_nodes host values */
+int goal_mechanics_get_solution(goal_mechanics m, double* U);
+/* DWR weights for the error chain: z_diff and z_coarse, 4*num_nodes each
+ * (u_z_diff/p_z_diff and p_z_coarse, src/goal_nested_adjoint.cpp:52-72) */
+int goal_mechanics_set_weights(goal_mechanics m, const double* z_diff, const double* z_coarse);
+/* state fields; sigma/Fp/Fp_old: 9*num_elems, eqps/eqps_old: num_elems */
+int goal_states_set(goal_mechanics m, int which, const double* values);
+int goal_states_get(goal_mechanics m, int which, double* values);
+/* States::update: Fp_old = Fp, eqps_old = eqps (src/goal_states.cpp:130-141) */
+int goal_states_update(goal_mechanics m);
+int goal_mechanics_destroy(goal_mechanics m);
+
+/* ---------------------------------------------------------------- SolInfo
+ * goal::create_sol_info (src/goal_sol_info.hpp:41): R, dMdu and dRdu. dRdu is
+ * stored as 4x4 blocks on the node graph; the CSR values in the order of
+ * goal_disc_get_graph are produced on request. */
+int goal_sol_info_create(goal_disc d, goal_sol_info* out);
+int goal_sol_info_zero_all(goal_sol_info s);
+int goal_sol_info_get_vector(goal_sol_info s, int which, double* values);
+int goal_sol_info_set_vector(goal_sol_info s, int which, const double* values);
+int goal_sol_info_get_dRdu_csr(goal_sol_info s, double* values);
+int goal_sol_info_get_dRdu_bsr(goal_sol_info s, double* values);
+int goal_sol_info_destroy(goal_sol_info s);
+
+/* ---------------------------------------------------------------- assemble
+ * assemble(Evaluators, SolInfo*) (src/goal_assembly.cpp:65-88) for the chains
+ * goal builds:
+ *   Primal residual   {PRIMAL, jacobian 0, save 1}  (src/goal_primal.cpp:75-90)
+ *   Primal jacobian   {PRIMAL, jacobian 1, save 1}  (src/goal_primal.cpp:92-109)
+ *   Functional        {NONE, jacobian 0, save 0, qoi} (src/goal_functional.cpp:62-70)
+ *   Nested adjoint    {ADJOINT, jacobian 1, save 0, qoi} (src/goal_nested_adjoint.cpp:163-180)
+ *   Error             {PRIMAL, jacobian 0, save 0, error_chain 1} (src/goal_nested_adjoint.cpp:217-234)
+ * overwrite = 1 makes the assembly start its outputs from zero (the zero_*
+ * calls that precede every assembly in goal); 0 accumulates into them. */
+typedef struct {
+  int mode;
+  int jacobian;
+  int save_states;
+  int qoi;
+  double rho;
+  int error_chain;
+  int overwrite;
+} goal_chain;
+int goal_assemble(goal_mechanics m, goal_sol_info s, const goal_chain* chain, double* qoi_value);
+
+/* ---------------------------------------------------------------- boundary conditions
+ * "dirichlet bcs: [eq, node set, expr]" and "traction bcs: [side set, Tx, Ty, Tz]". */
+int goal_bcs_create(goal_disc d, goal_bcs* out);
+int goal_bcs_add_dirichlet(goal_bcs b, int eq, const char* node_set, const char* expr);
+int goal_bcs_add_traction(goal_bcs b, const char* side_set, const char* tx, const char* ty, const char* tz);
+int goal_bcs_destroy(goal_bcs b);
+/* set_resid_dbcs / set_jac_dbcs (src/goal_dbcs.cpp:39-99) */
+int goal_set_resid_dbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t);
+int goal_set_jac_dbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t);
+/* set_tbcs (src/goal_tbcs.cpp:29-85); error_weights = 1 uses the z_diff weights */
+int goal_set_tbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t, int error_weights);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GOAL_GB300_H */
