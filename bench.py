@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""Benchmark: element R+J assembly throughput of goal's J2 mixed u-p chain.
+
+Workload (the production-size configuration): the unit cube meshed as a 40^3
+hex grid split into 6 Kuhn tets per hex (384,000 tets, 68,921 nodes, 275,684
+dofs, 15.9M CSR nonzeros), J2 finite-strain plasticity E=200e3, nu=0.3, Y=250,
+K=1000, c0=1, stabilized mixed u-p, FP64. A step is one pass of the primal
+Jacobian chain (residual, hand-derived tangent scattered into the 4x4-block
+matrix, integration-point state update) over every element, i.e. goal's
+assemble() with the FADT evaluators (src/goal_primal.cpp:92-109).
+
+Synthetic seeded inputs stand in for a load step's state: u = a (sin pi x,
+sin pi y, sin pi z) + N(0, (0.1 a)^2) noise with a = c 1e-3, p ~ N(0, 1),
+Fp_old = expm(c 1e-3 sym(G)), eqps_old ~ U[0, 0.01], with the factor c set so
+that about half of the integration points yield. The working set (matrix values 127 MB, states,
+geometry) is larger than the 126 MB L2, so no flush is needed between steps.
+
+Prints one JSON line. --impl reference times the CPU restatement of the same
+chain (forward-mode dual numbers, all host threads) instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elem/s R+J assembly; adjoint solve s to 1e-10 rel: learned+mixed vs plain FP64"
+MAT = dict(E=200e3, nu=0.3, K=1000.0, Y=250.0, c0=1.0)
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=40, help="hexes per cube edge")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ workload
+class YieldProbe:
+    """Vectorized trial-state check of the J2 yield condition (elastic predictor)
+    over all elements, with the element geometry computed once."""
+
+    def __init__(self, mesh):
+        x = mesh.coords
+        t = mesh.tets
+        Jm = np.stack([x[t[:, 1]] - x[t[:, 0]], x[t[:, 2]] - x[t[:, 0]], x[t[:, 3]] - x[t[:, 0]]], axis=2)
+        Ji = np.linalg.inv(Jm)
+        self.G = np.concatenate([-Ji.sum(axis=1, keepdims=True), Ji], axis=1)  # (E,4,3)
+        self.t = t
+
+    def fraction(self, u, Fp_old, eqps_old):
+        mu = MAT["E"] / (2 * (1 + MAT["nu"]))
+        F = np.eye(3) + np.einsum("eai,eaj->eij", u[self.t], self.G)
+        J = np.linalg.det(F)
+        Fpi = np.linalg.inv(Fp_old)
+        C = Fpi @ np.transpose(Fpi, (0, 2, 1))
+        B = F @ C @ np.transpose(F, (0, 2, 1))
+        Ic = np.trace(B, axis1=1, axis2=2)
+        s = mu * J[:, None, None] ** (-2.0 / 3.0) * (B - Ic[:, None, None] / 3 * np.eye(3))
+        smag = np.sqrt((s * s).sum(axis=(1, 2)))
+        f = smag - np.sqrt(2 / 3) * (MAT["Y"] + MAT["K"] * eqps_old)
+        return float((f > 1e-12).mean())
+
+
+def workload(n, seed=0):
+    """Kuhn cube mesh and a seeded state: u = c a0 (sin pi x, sin pi y, sin pi z)
+    + noise, Fp_old = expm(c eps0 sym(G)), eqps_old ~ U[0, 0.01]; the common
+    factor c is bisected so that about half of the points yield."""
+    from goal_gb300.mesh import kuhn_cube
+    mesh = kuhn_cube(n)
+    rng = np.random.default_rng(seed)
+    x = mesh.coords
+    shape = np.stack([np.sin(np.pi * x[:, 0]), np.sin(np.pi * x[:, 1]), np.sin(np.pi * x[:, 2])], axis=1)
+    noise = rng.standard_normal(shape.shape)
+    G = rng.standard_normal((mesh.num_elems, 3, 3))
+    w, Q = np.linalg.eigh(0.5 * (G + np.transpose(G, (0, 2, 1))))
+    eqps_old = rng.uniform(0.0, 0.01, mesh.num_elems)
+    p = rng.standard_normal(mesh.num_nodes)
+    a0, eps0 = 1e-3, 1e-3
+    probe = YieldProbe(mesh)
+
+    def state(c):
+        u = c * a0 * (shape + 0.1 * noise)
+        Fp = np.einsum("eij,ej,ekj->eik", Q, np.exp(c * eps0 * w), Q)
+        return u, Fp
+
+    lo, hi = 1e-2, 1e2
+    for _ in range(16):
+        c = np.sqrt(lo * hi)
+        u, Fp = state(c)
+        if probe.fraction(u, Fp, eqps_old) > 0.5:
+            hi = c
+        else:
+            lo = c
+    c = np.sqrt(lo * hi)
+    u, Fp = state(c)
+    frac = probe.fraction(u, Fp, eqps_old)
+    return mesh, u, p, Fp.reshape(-1, 9), eqps_old, c, frac
+
+
+def algorithmic_bytes(num_nodes, num_elems, nnz, state_bytes=232):
+    """Compulsory traffic of one R+J assembly: connectivity 16 B/elem, coordinates
+    and u,p 56 B/node, R 32 B/node, matrix values 8 B/nnz written once, J2
+    states 80 B read + 152 B written per element."""
+    return 16 * num_elems + 56 * num_nodes + 32 * num_nodes + 8 * nnz + state_bytes * num_elems
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self, gpu_index=0):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [q.strip() for q in line.split(",")]
+                if len(parts) < 9 or parts[0] != str(gpu_index):
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = max(mx, float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() in ("active", "1"):
+                        reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_assembly_rate(mesh, u, p, Fp_old, eqps_old, seconds, threads):
+    """Oracle (CPU restatement, dual-number Jacobian) on a bounded sample of the
+    workload's elements; returns (elem/s, elements timed)."""
+    from oracle import oracle as O
+    from goal_gb300.mesh import Mesh
+    mat = O.Material(MAT["E"], MAT["nu"], K=MAT["K"], Y=MAT["Y"], c0=MAT["c0"])
+    g = O.csr_graph(mesh.num_nodes, mesh.tets)
+    chunk = 4096
+    done, t_used = 0, 0.0
+    R = np.zeros(4 * mesh.num_nodes)
+    vals = np.zeros(len(g[1]))
+    while t_used < seconds and done < mesh.num_elems:
+        e0, e1 = done, min(done + chunk, mesh.num_elems)
+        sub = Mesh(coords=mesh.coords, tets=np.ascontiguousarray(mesh.tets[e0:e1]),
+                   elem_set=np.zeros(e1 - e0, np.int32), elem_set_names=["cube"], node_sets={}, side_sets={})
+        st = O.States.initial(e1 - e0)
+        st.Fp_old[:] = Fp_old[e0:e1]
+        st.eqps_old[:] = eqps_old[e0:e1]
+        t0 = time.perf_counter()
+        O.assemble(sub, O.J2, [mat], u, p, st, mode=O.PRIMAL, fad=True, save=True, graph=g, R=R, vals=vals,
+                   threads=threads)
+        t_used += time.perf_counter() - t0
+        done = e1
+        chunk = min(chunk * 2, 65536)
+    return done / t_used, done
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    mesh, u, p, Fp_old, eqps_old, amp, frac = workload(a.n)
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    per_step = max(1.0, 60.0 / max(1, a.steps + a.warmup))
+    for _ in range(a.warmup):
+        cpu_assembly_rate(mesh, u, p, Fp_old, eqps_old, min(per_step, 2.0), True)
+    rates, elems = [], 0
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        r, ne = cpu_assembly_rate(mesh, u, p, Fp_old, eqps_old, per_step, True)
+        rates.append(r)
+        elems += ne
+    wall = time.perf_counter() - t0
+    value = elems / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "elem/s", "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1000.0 * wall / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"kuhn cube {a.n}^3 x 6 tets, J2 mixed u-p, primal R+J assembly",
+                   "elements": mesh.num_elems, "nodes": mesh.num_nodes, "yield_fraction": frac},
+        "cpu_baseline": {"value": value, "unit": "elem/s", "cores": threads, "kind": "port",
+                         "sample": f"{elems} element evaluations over {a.steps} steps (bounded samples of the mesh), "
+                                   f"dual-number Jacobian, OpenMP element loop + serial scatter"},
+        "e2e": {"value": value, "unit": "elem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU leg
+def main():
+    a = _args()
+    if a.impl == "reference":
+        return run_reference(a)
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    from goal_gb300 import api, lib
+    L = lib()
+
+    mesh, u, p, Fp_old, eqps_old, amp, frac = workload(a.n)
+    d = api.Disc(mesh)
+    m = api.Mechanics(d, api.J2, [[MAT["E"], MAT["nu"], MAT["K"], MAT["Y"], MAT["c0"]]])
+    U = np.zeros((mesh.num_nodes, 4))
+    U[:, :3] = u
+    U[:, 3] = p
+    m.set_solution(U.ravel())
+    m.set_state(api.FP_OLD, Fp_old)
+    m.set_state(api.EQPS_OLD, eqps_old)
+    s = api.SolInfo(d)
+    stream = torch.cuda.ExternalStream(d.stream())
+
+    def step():
+        api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=True)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(max(3, a.warmup)):
+        step()
+    barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches0 = L.goal_launch_count()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        step()
+    ev1.record(stream)
+    ev1.synchronize()
+    launches = L.goal_launch_count() - launches0
+    barrier()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end through the public API: pinned host U in, host R out, every step
+    Uh = torch.from_numpy(U.ravel().copy()).pin_memory()
+    Rh = torch.empty(4 * mesh.num_nodes, dtype=torch.float64).pin_memory()
+    import ctypes
+    for _ in range(2):
+        L.goal_mechanics_set_solution(m.h, ctypes.c_void_p(Uh.data_ptr()))
+        step()
+        L.goal_sol_info_get_vector(s.h, 0, ctypes.c_void_p(Rh.data_ptr()))
+    barrier()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        L.goal_mechanics_set_solution(m.h, ctypes.c_void_p(Uh.data_ptr()))
+        step()
+        L.goal_sol_info_get_vector(s.h, 0, ctypes.c_void_p(Rh.data_ptr()))
+    e1.record(stream)
+    e1.synchronize()
+    e2e_ms = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0)) / a.steps
+    barrier()
+    clk = clocks.stop(local)
+
+    if rank != 0:
+        return 0
+    E = mesh.num_elems
+    value = world * E / (ms * 1e-3)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peaks = json.load(f)
+        hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    else:
+        hbm_peak, peak_src = 6800.0, "fallback"
+    alg = algorithmic_bytes(mesh.num_nodes, E, d.nnz)
+    achieved = alg / (ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "elem_j2_primal_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            pr = json.load(f)
+        traffic = pr["dram_bytes_per_element"] * E
+    line = {
+        "metric": METRIC, "value": value, "unit": "elem/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"kuhn cube {a.n}^3 x 6 tets, J2 mixed u-p, primal R+J assembly",
+                   "elements": E, "nodes": mesh.num_nodes, "nnz": d.nnz, "colors": d.num_colors,
+                   "yield_fraction": round(frac, 4), "l2": "working set > L2 (no flush)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": world * E / (e2e_ms * 1e-3), "unit": "elem/s", "h2d_bytes_per_step": 8 * 4 * mesh.num_nodes,
+                "d2h_bytes_per_step": 8 * 4 * mesh.num_nodes},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                     "algorithmic_bytes_per_step": alg},
+        "clocks": clk,
+    }
+    if not a.no_cpu_baseline:
+        rate, ne = cpu_assembly_rate(mesh, u, p, Fp_old, eqps_old, a.cpu_seconds, False)
+        line["cpu_baseline"] = {"value": rate, "unit": "elem/s", "cores": 1, "kind": "port",
+                                "sample": f"first {ne} elements of the same mesh and states, dual-number Jacobian "
+                                          f"(16 slots), binary-search scatter, 1 thread"}
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -14,6 +14,34 @@ class Chain(ctypes.Structure):
                 ("overwrite", ctypes.c_int)]
 
 
+class SolveParams(ctypes.Structure):
+    """goal_solve_params"""
+    _fields_ = [("krylov_size", ctypes.c_int), ("max_iters", ctypes.c_int), ("tolerance", ctypes.c_double),
+                ("precision", ctypes.c_int), ("inner_iters", ctypes.c_int), ("precond", ctypes.c_int),
+                ("learned_cap", ctypes.c_int)]
+
+
+class SolveStats(ctypes.Structure):
+    """goal_solve_stats"""
+    _fields_ = [("iters", ctypes.c_int), ("inner_iters", ctypes.c_int), ("converged", ctypes.c_int),
+                ("fell_back", ctypes.c_int), ("rel_res", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("spmv64", ctypes.c_longlong), ("spmv32", ctypes.c_longlong)]
+
+
+class NewtonStats(ctypes.Structure):
+    """goal_newton_stats"""
+    _fields_ = [("iters", ctypes.c_int), ("converged", ctypes.c_int), ("linear_iters", ctypes.c_int),
+                ("inner_iters", ctypes.c_int), ("norms", ctypes.c_double * 32),
+                ("seconds_assembly", ctypes.c_double), ("seconds_solve", ctypes.c_double)]
+
+
+class DwrResult(ctypes.Structure):
+    """goal_dwr_result"""
+    _fields_ = [("eta", ctypes.c_double), ("bound", ctypes.c_double), ("qoi", ctypes.c_double),
+                ("solve", SolveStats), ("seconds_adjoint", ctypes.c_double), ("seconds_solve", ctypes.c_double),
+                ("seconds_localize", ctypes.c_double)]
+
+
 def parse_header(path: str = HEADER):
     """Returns {name: (return type, [argument types])} for every function declared."""
     with open(path) as f:

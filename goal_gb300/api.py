@@ -14,7 +14,7 @@ from typing import Iterable, Optional, Sequence, Tuple
 import numpy as np
 
 from . import lib
-from ._abi import Chain
+from ._abi import Chain, DwrResult, NewtonStats, SolveParams, SolveStats
 
 NONE, PRIMAL, ADJOINT = 0, 1, 2          # goal::EvalModes
 NEOHOOKEAN, J2 = 0, 1
@@ -275,3 +275,92 @@ def eval_expr(expr: str, x: float, y: float, z: float, t: float) -> float:
     out = ctypes.c_double()
     check(lib().goal_eval(expr.encode(), x, y, z, t, ctypes.byref(out)))
     return out.value
+
+
+FP64, MIXED = 0, 1
+PRECOND_BJ, PRECOND_LEARNED = 0, 1
+
+
+def solve_params(krylov_size=100, max_iters=2000, tolerance=1e-10, precision=FP64, inner_iters=30,
+                 precond=PRECOND_BJ, learned_cap=0) -> SolveParams:
+    return SolveParams(krylov_size=krylov_size, max_iters=max_iters, tolerance=tolerance, precision=precision,
+                       inner_iters=inner_iters, precond=precond, learned_cap=learned_cap)
+
+
+def _stats_dict(st: SolveStats) -> dict:
+    return dict(iters=st.iters, inner_iters=st.inner_iters, converged=bool(st.converged), fell_back=bool(st.fell_back),
+                rel_res=st.rel_res, seconds=st.seconds, spmv64=st.spmv64, spmv32=st.spmv32)
+
+
+def solve(sol_info: SolInfo, b: np.ndarray, x0: Optional[np.ndarray] = None, params: Optional[SolveParams] = None):
+    """goal::solve on dRdu of the SolInfo; returns (x, stats)."""
+    b = _f64(b).reshape(-1)
+    x = np.zeros_like(b) if x0 is None else _f64(x0).reshape(-1).copy()
+    st = SolveStats()
+    check(lib().goal_solve(sol_info.h, ctypes.byref(params or solve_params()), _ptr(b), _ptr(x), ctypes.byref(st)))
+    return x, _stats_dict(st)
+
+
+def primal_solve(mech: Mechanics, s: SolInfo, bcs: Bcs, t_now: float, t_old: float, max_iters: int = 5,
+                 tolerance: float = 1e-8, params: Optional[SolveParams] = None) -> dict:
+    """Primal::solve (Newton); raises GoalError(GOAL_ERR_NEWTON) when it fails."""
+    st = NewtonStats()
+    check(lib().goal_primal_solve(mech.h, s.h, bcs.h, t_now, t_old, max_iters, tolerance,
+                                  ctypes.byref(params or solve_params()), ctypes.byref(st)))
+    return dict(iters=st.iters, converged=bool(st.converged), linear_iters=st.linear_iters,
+                inner_iters=st.inner_iters, norms=list(st.norms[:st.iters]),
+                seconds_assembly=st.seconds_assembly, seconds_solve=st.seconds_solve)
+
+
+class NestedAdjoint:
+    """NestedAdjoint: adjoint on the uniformly refined mesh and the DWR estimate."""
+
+    def __init__(self, base_mech: Mechanics, dirichlet=(), traction=()):
+        h = ctypes.c_void_p()
+        check(lib().goal_nested_adjoint_create(base_mech.h, ctypes.byref(h)))
+        self.h = h
+        self.base = base_mech
+        dh = ctypes.c_void_p()
+        check(lib().goal_nested_adjoint_disc(self.h, ctypes.byref(dh)))
+        self.disc = Disc.__new__(Disc)
+        self.disc._base = base_mech.disc
+        self.disc.mesh = None
+        self.disc.h = dh
+        sizes = np.zeros(6, np.int64)
+        check(lib().goal_disc_sizes(dh, _ptr(sizes)))
+        (self.disc.num_nodes, self.disc.num_elems, self.disc.num_dofs, self.disc.nnz, self.disc.nnzb,
+         self.disc.num_colors) = (int(x) for x in sizes)
+        self.bcs = Bcs(self.disc, dirichlet, traction)
+
+    def run(self, qoi: int, rho: float, t_now: float, t_old: float, params: Optional[SolveParams] = None,
+            nested_error: bool = False) -> dict:
+        r = DwrResult()
+        be = np.zeros(self.base.disc.num_elems)
+        ne = np.zeros(self.disc.num_elems) if nested_error else None
+        check(lib().goal_nested_adjoint_run(self.h, self.bcs.h, qoi, rho, t_now, t_old,
+                                            ctypes.byref(params or solve_params()), ctypes.byref(r), _ptr(be),
+                                            _ptr(ne)))
+        out = dict(eta=r.eta, bound=r.bound, qoi=r.qoi, solve=_stats_dict(r.solve), base_error=be,
+                   seconds_adjoint=r.seconds_adjoint, seconds_solve=r.seconds_solve,
+                   seconds_localize=r.seconds_localize)
+        if ne is not None:
+            out["nested_error"] = ne
+        return out
+
+    def z(self) -> np.ndarray:
+        z = np.zeros(self.disc.num_dofs)
+        check(lib().goal_nested_adjoint_get_z(self.h, _ptr(z)))
+        return z
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.bcs.close()
+            self.disc.h = None  # owned by the nested adjoint
+            lib().goal_nested_adjoint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

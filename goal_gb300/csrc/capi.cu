@@ -6,6 +6,7 @@
 
 #include "../../include/goal_gb300.h"
 #include "capi_internal.cuh"
+#include "driver.cuh"
 
 namespace goal {
 
@@ -118,6 +119,43 @@ struct goal_bcs_s {
   std::vector<DBC> dbcs;
   std::vector<TBC> tbcs;
 };
+struct goal_nested_adjoint_s {
+  NestedAdjoint a;
+  goal_disc_s disc_view;  // non-owning view handed to goal_nested_adjoint_disc
+  ~goal_nested_adjoint_s() { disc_view.d.release(); }
+};
+
+static SolveParams to_params(const goal_solve_params* p) {
+  SolveParams q;
+  if (p) {
+    q.krylov_size = p->krylov_size;
+    q.max_iters = p->max_iters;
+    q.tolerance = p->tolerance;
+    q.precision = p->precision;
+    q.inner_iters = p->inner_iters;
+    q.precond = p->precond;
+    q.learned_cap = p->learned_cap;
+  }
+  GOAL_REQUIRE(q.krylov_size >= 1 && q.krylov_size < 256, GOAL_ERR_ARG, "krylov size must be in [1, 255]");
+  GOAL_REQUIRE(q.max_iters >= 1, GOAL_ERR_ARG, "max iters must be >= 1");
+  GOAL_REQUIRE(q.tolerance > 0.0, GOAL_ERR_ARG, "tolerance must be > 0");
+  GOAL_REQUIRE(q.precision == PREC_FP64 || q.precision == PREC_MIXED, GOAL_ERR_ARG, "unknown precision mode");
+  GOAL_REQUIRE(q.precision == PREC_FP64 || (q.inner_iters >= 1 && q.inner_iters < 256), GOAL_ERR_ARG,
+               "inner iterations must be in [1, 255]");
+  return q;
+}
+
+static void to_stats(const SolveStats& s, goal_solve_stats* o) {
+  if (!o) return;
+  o->iters = s.iters;
+  o->inner_iters = s.inner_iters;
+  o->converged = s.converged;
+  o->fell_back = s.fell_back;
+  o->rel_res = s.rel_res;
+  o->seconds = s.seconds;
+  o->spmv64 = s.spmv64;
+  o->spmv32 = s.spmv32;
+}
 
 #define GOAL_API_BEGIN try {
 #define GOAL_API_END                                      \
@@ -517,6 +555,113 @@ int goal_set_tbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t, int e
   }
   apply_tbcs(*m->m, *s->s, b->tbcs, t, zd, m->m->disc->stream);
   GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_solve_device(goal_sol_info s, const goal_solve_params* params, const double* b, double* x,
+                      goal_solve_stats* stats) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s && b && x, "goal_solve: null argument");
+  SolveParams p = to_params(params);
+  static thread_local Krylov K;
+  SolveStats r = linear_solve(*s->s, p, b, x, K);
+  to_stats(r, stats);
+  GOAL_REQUIRE(r.rel_res == r.rel_res, GOAL_ERR_SOLVER, "linear solve produced a non-finite residual");
+  GOAL_API_END
+}
+
+int goal_solve(goal_sol_info s, const goal_solve_params* params, const double* b, double* x, goal_solve_stats* stats) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s && b && x, "goal_solve: null argument");
+  cudaStream_t st = s->s->disc->stream;
+  size_t n = 4ull * s->s->disc->num_nodes;
+  DevBuf<double> db, dx;
+  db.upload(b, n, st);
+  dx.upload(x, n, st);
+  int rc = goal_solve_device(s, params, db.ptr, dx.ptr, stats);
+  if (rc) return rc;
+  dx.download(x, st);
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  GOAL_API_END
+}
+
+int goal_primal_solve(goal_mechanics m, goal_sol_info s, goal_bcs b, double t_now, double t_old, int max_iters,
+                      double tolerance, const goal_solve_params* lin, goal_newton_stats* stats) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && s && b && b->d == m->m->disc && s->s->disc == m->m->disc, "goal_primal_solve: bad arguments");
+  NewtonParams p;
+  p.max_iters = max_iters;
+  p.tolerance = tolerance;
+  p.lin = to_params(lin);
+  static thread_local Krylov K;
+  NewtonStats r = primal_solve(*m->m, *s->s, b->dbcs, b->tbcs, t_now, t_old, p, K);
+  if (stats) {
+    stats->iters = r.iters;
+    stats->converged = r.converged;
+    stats->linear_iters = r.linear_iters;
+    stats->inner_iters = r.inner_iters;
+    for (int i = 0; i < 32; ++i) stats->norms[i] = r.norms[i];
+    stats->seconds_assembly = r.seconds_assembly;
+    stats->seconds_solve = r.seconds_solve;
+  }
+  GOAL_REQUIRE(r.converged, GOAL_ERR_NEWTON,
+               "newton's method failed in " + std::to_string(max_iters) + " iterations");
+  GOAL_API_END
+}
+
+int goal_nested_adjoint_create(goal_mechanics base, goal_nested_adjoint* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(base && out, "null argument");
+  auto h = std::make_unique<goal_nested_adjoint_s>();
+  h->a.build(*base->m);
+  h->disc_view.d.reset(h->a.disc.get());
+  h->disc_view.owns_stream = false;
+  *out = h.release();
+  GOAL_API_END
+}
+
+int goal_nested_adjoint_disc(goal_nested_adjoint a, goal_disc* nested) {
+  GOAL_API_BEGIN
+  GOAL_ARG(a && nested, "null argument");
+  *nested = &a->disc_view;
+  GOAL_API_END
+}
+
+int goal_nested_adjoint_run(goal_nested_adjoint a, goal_bcs nested_bcs, int qoi, double rho, double t_now,
+                            double t_old, const goal_solve_params* params, goal_dwr_result* result,
+                            double* base_error, double* nested_error) {
+  GOAL_API_BEGIN
+  GOAL_ARG(a && nested_bcs && nested_bcs->d == a->a.disc.get(), "goal_nested_adjoint_run: bcs must be on the nested disc");
+  GOAL_ARG(qoi == GOAL_QOI_AVG_DISP || qoi == GOAL_QOI_KS_VM, "goal_nested_adjoint_run: unknown functional");
+  SolveParams p = to_params(params);
+  DwrResult r = nested_adjoint_run(a->a, nested_bcs->dbcs, nested_bcs->tbcs, qoi, rho, t_now, t_old, p);
+  if (result) {
+    result->eta = r.eta;
+    result->bound = r.bound;
+    result->qoi = r.qoi;
+    to_stats(r.solve, &result->solve);
+    result->seconds_adjoint = r.seconds_adjoint;
+    result->seconds_solve = r.seconds_solve;
+    result->seconds_localize = r.seconds_localize;
+  }
+  cudaStream_t st = a->a.disc->stream;
+  if (base_error) a->a.err_base.download(base_error, st);
+  if (nested_error) a->a.err_nested.download(nested_error, st);
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  GOAL_API_END
+}
+
+int goal_nested_adjoint_get_z(goal_nested_adjoint a, double* z) {
+  GOAL_API_BEGIN
+  GOAL_ARG(a && z, "null argument");
+  a->a.z.download(z, a->a.disc->stream);
+  GOAL_CUDA(cudaStreamSynchronize(a->a.disc->stream));
+  GOAL_API_END
+}
+
+int goal_nested_adjoint_destroy(goal_nested_adjoint a) {
+  GOAL_API_BEGIN
+  delete a;
   GOAL_API_END
 }
 

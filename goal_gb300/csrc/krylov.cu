@@ -1,0 +1,648 @@
+// Device-resident FGMRES on 4x4-block matrices (see krylov.cuh).
+//
+// Iteration state (column count j, done flag, reorthogonalization flag,
+// residual estimate) lives in device memory, so one Arnoldi step is a fixed
+// sequence of kernels that never waits for the host: the host enqueues steps
+// and reads the residual estimate once per step.
+#include <chrono>
+#include <cmath>
+
+#include "krylov.cuh"
+
+namespace goal {
+
+namespace {
+
+struct GState {
+  int j;        // completed Arnoldi columns in this cycle
+  int done;     // 1: converged, broke down or restart length reached
+  int reorth;   // second Gram-Schmidt pass needed for the current column
+  int pad;
+  double wb2;   // |w|^2 before orthogonalization
+  double res;   // |g[j]| residual estimate
+  double beta;  // initial residual norm of the cycle
+};
+
+constexpr int kMaxM = 256;
+constexpr int kDotChunk = 8;
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<double> {
+  static __device__ __forceinline__ void load(const double* p, double& a, double& b, double& c, double& d) {
+    double4_32a v = *reinterpret_cast<const double4_32a*>(p);
+    a = v.x; b = v.y; c = v.z; d = v.w;
+  }
+};
+template <>
+struct Vec4<float> {
+  static __device__ __forceinline__ void load(const float* p, float& a, float& b, float& c, float& d) {
+    float4 v = *reinterpret_cast<const float4*>(p);
+    a = v.x; b = v.y; c = v.z; d = v.w;
+  }
+};
+
+// y = A x  (or y = b - A x). One warp per block row; lane = 4*slot + row.
+template <typename T, bool RESID>
+__global__ void __launch_bounds__(256) k_spmv(int N, const int* __restrict__ brow_ptr, const int* __restrict__ bcol,
+                                              const T* __restrict__ A, const T* __restrict__ x,
+                                              const T* __restrict__ b, T* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int slot = lane >> 2, r = lane & 3;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += nw) {
+    const int b0 = __ldg(brow_ptr + n), b1 = __ldg(brow_ptr + n + 1);
+    T acc = T(0);
+    for (int k = b0 + slot; k < b1; k += 8) {
+      const int c = __ldg(bcol + k);
+      T a0, a1, a2, a3, x0, x1, x2, x3;
+      Vec4<T>::load(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+      Vec4<T>::load(x + 4ll * c, x0, x1, x2, x3);
+      acc += a0 * x0 + a1 * x1 + a2 * x2 + a3 * x3;
+    }
+    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 8);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 16);
+    if (lane < 4) {
+      if (RESID) y[4ll * n + lane] = b[4ll * n + lane] - acc;
+      else y[4ll * n + lane] = acc;
+    }
+  }
+}
+
+// z = Dinv v for node blocks (one thread per row); column j of V/Z from the state.
+template <typename T>
+__global__ void k_bj_col(int N, const T* __restrict__ Dinv, const T* V, T* Z, long long ld, const GState* st) {
+  if (st->done) return;
+  const long long off = (long long)st->j * ld;
+  const T* v = V + off;
+  T* z = Z + off;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 2, r = i & 3;
+    T d0, d1, d2, d3, x0, x1, x2, x3;
+    Vec4<T>::load(Dinv + 16ll * n + 4 * r, d0, d1, d2, d3);
+    Vec4<T>::load(v + 4ll * n, x0, x1, x2, x3);
+    z[i] = d0 * x0 + d1 * x1 + d2 * x2 + d3 * x3;
+  }
+}
+
+// out = Dinv v_j with v_j = column j of V
+template <typename T>
+__global__ void k_bj_colin(int N, const T* __restrict__ Dinv, const T* V, long long ld, const GState* st,
+                           T* __restrict__ out) {
+  if (st->done) return;
+  const T* v = V + (long long)st->j * ld;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 2, r = i & 3;
+    T d0, d1, d2, d3, x0, x1, x2, x3;
+    Vec4<T>::load(Dinv + 16ll * n + 4 * r, d0, d1, d2, d3);
+    Vec4<T>::load(v + 4ll * n, x0, x1, x2, x3);
+    out[i] = d0 * x0 + d1 * x1 + d2 * x2 + d3 * x3;
+  }
+}
+
+template <typename T>
+__global__ void k_bj(int N, const T* __restrict__ Dinv, const T* __restrict__ v, T* __restrict__ z) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 2, r = i & 3;
+    T d0, d1, d2, d3, x0, x1, x2, x3;
+    Vec4<T>::load(Dinv + 16ll * n + 4 * r, d0, d1, d2, d3);
+    Vec4<T>::load(v + 4ll * n, x0, x1, x2, x3);
+    z[i] = d0 * x0 + d1 * x1 + d2 * x2 + d3 * x3;
+  }
+}
+
+// w = A z_j with z_j = column j of Z
+template <typename T>
+__global__ void __launch_bounds__(256) k_spmv_col(int N, const int* __restrict__ brow_ptr,
+                                                  const int* __restrict__ bcol, const T* __restrict__ A,
+                                                  const T* Z, long long ld, const GState* st, T* __restrict__ y) {
+  if (st->done) return;
+  const T* x = Z + (long long)st->j * ld;
+  const int lane = threadIdx.x & 31;
+  const int slot = lane >> 2, r = lane & 3;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += nw) {
+    const int b0 = __ldg(brow_ptr + n), b1 = __ldg(brow_ptr + n + 1);
+    T acc = T(0);
+    for (int k = b0 + slot; k < b1; k += 8) {
+      const int c = __ldg(bcol + k);
+      T a0, a1, a2, a3, x0, x1, x2, x3;
+      Vec4<T>::load(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+      Vec4<T>::load(x + 4ll * c, x0, x1, x2, x3);
+      acc += a0 * x0 + a1 * x1 + a2 * x2 + a3 * x3;
+    }
+    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 8);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 16);
+    if (lane < 4) y[4ll * n + lane] = acc;
+  }
+}
+
+// partial dot products of w with columns 0..j of V and with itself (column j+1)
+template <typename T>
+__global__ void __launch_bounds__(256) k_multidot(long long n, const T* V, long long ld, const T* __restrict__ w,
+                                                  const GState* st, double* part, int pass) {
+  if (st->done) return;
+  if (pass == 1 && !st->reorth) return;
+  const int j = st->j;
+  const int c0 = blockIdx.y * kDotChunk;
+  const int ncols = j + 2;
+  if (c0 >= ncols) return;
+  T acc[kDotChunk];
+#pragma unroll
+  for (int q = 0; q < kDotChunk; ++q) acc[q] = T(0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const T wi = w[i];
+#pragma unroll
+    for (int q = 0; q < kDotChunk; ++q) {
+      const int c = c0 + q;
+      if (c <= j) acc[q] += V[c * ld + i] * wi;
+      else if (c == j + 1) acc[q] += wi * wi;
+    }
+  }
+  __shared__ double sm[kDotChunk][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kDotChunk; ++q) {
+    double v = (double)acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sm[q][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kDotChunk) {
+    const int q = threadIdx.x;
+    double v = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) v += sm[q][k];
+    const int c = c0 + q;
+    if (c < ncols) part[(long long)c * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+__global__ void k_dots_fin(int nbx, const double* part, GState* st, double* H, int ldh, double* dots, int pass) {
+  if (st->done) return;
+  if (pass == 1 && !st->reorth) return;
+  const int j = st->j;
+  const int c = blockIdx.x;
+  if (c > j + 1) return;
+  double v = 0.0;
+  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[(long long)c * nbx + k];
+  __shared__ double sm[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
+    if (c <= j) {
+      dots[c] = s;
+      if (pass == 0) H[c + (long long)ldh * j] = s;
+      else H[c + (long long)ldh * j] += s;
+    } else if (pass == 0) {
+      st->wb2 = s;
+    }
+  }
+}
+
+// w -= V dots ; partial |w|^2
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(long long n, const T* V, long long ld, T* w, const double* dots,
+                                                const GState* st, double* part, int pass) {
+  if (st->done) return;
+  if (pass == 1 && !st->reorth) return;
+  const int j = st->j;
+  __shared__ T sd[kMaxM + 1];
+  for (int c = threadIdx.x; c <= j; c += blockDim.x) sd[c] = (T)dots[c];
+  __syncthreads();
+  T acc = T(0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    T v = w[i];
+    for (int c = 0; c <= j; ++c) v -= sd[c] * V[c * ld + i];
+    w[i] = v;
+    acc += v * v;
+  }
+  double a = (double)acc;
+  __shared__ double sm[32];
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
+    part[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_norm_fin(int nbx, const double* part, GState* st, double* H, int ldh, int pass) {
+  if (st->done) return;
+  if (pass == 1 && !st->reorth) return;
+  double v = 0.0;
+  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
+  __shared__ double sm[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
+    const int j = st->j;
+    if (pass == 0) st->reorth = (s < 0.5 * st->wb2) ? 1 : 0;
+    H[j + 1 + (long long)ldh * j] = sqrt(s);
+  }
+}
+
+template <typename T>
+__global__ void k_normalize(long long n, T* V, long long ld, const T* w, const GState* st, const double* H, int ldh) {
+  if (st->done) return;
+  const int j = st->j;
+  const double h = H[j + 1 + (long long)ldh * j];
+  const T inv = (h > 0.0) ? (T)(1.0 / h) : T(0);
+  T* v = V + (long long)(j + 1) * ld;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v[i] = w[i] * inv;
+}
+
+__global__ void k_givens(GState* st, double* H, int ldh, double* cs, double* sn, double* g, int jmax, double tol_abs) {
+  if (st->done) return;
+  const int j = st->j;
+  double* h = H + (long long)ldh * j;
+  for (int i = 0; i < j; ++i) {
+    double t = cs[i] * h[i] + sn[i] * h[i + 1];
+    h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+    h[i] = t;
+  }
+  const double a = h[j], b = h[j + 1];
+  const double r = hypot(a, b);
+  double c = 1.0, s = 0.0;
+  if (r > 0.0) { c = a / r; s = b / r; }
+  cs[j] = c;
+  sn[j] = s;
+  h[j] = r;
+  h[j + 1] = 0.0;
+  g[j + 1] = -s * g[j];
+  g[j] = c * g[j];
+  st->res = fabs(g[j + 1]);
+  st->j = j + 1;
+  if (st->res <= tol_abs || st->j >= jmax || b == 0.0 || !(st->res == st->res)) st->done = 1;
+}
+
+__global__ void k_backsolve(const GState* st, const double* H, int ldh, const double* g, double* y) {
+  const int k = st->j;
+  for (int i = k - 1; i >= 0; --i) {
+    double s = g[i];
+    for (int c = i + 1; c < k; ++c) s -= H[i + (long long)ldh * c] * y[c];
+    const double d = H[i + (long long)ldh * i];
+    y[i] = (d != 0.0) ? s / d : 0.0;
+  }
+}
+
+template <typename T, typename TX>
+__global__ void k_combine(long long n, const T* Z, long long ld, const double* y, const GState* st, TX* x, int zero_first) {
+  const int k = st->j;
+  __shared__ double sy[kMaxM];
+  for (int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = y[c];
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double s = zero_first ? 0.0 : (double)x[i];
+    for (int c = 0; c < k; ++c) s += sy[c] * (double)Z[c * ld + i];
+    x[i] = (TX)s;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_norm2_part(long long n, const T* x, double* part) {
+  double a = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double v = (double)x[i];
+    a += v * v;
+  }
+  __shared__ double sm[32];
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
+    part[blockIdx.x] = s;
+  }
+}
+
+// beta = |r| from partials; V_0 = r / beta; g = [beta, 0, ...]; state reset
+__global__ void k_cycle_fin(int nbx, const double* part, GState* st, double* g, int m, double* out_beta) {
+  double v = 0.0;
+  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
+  __shared__ double sm[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
+    double beta = sqrt(s);
+    st->beta = beta;
+    st->j = 0;
+    st->reorth = 0;
+    st->res = beta;
+    st->done = (beta > 0.0 && beta == beta) ? 0 : 1;
+    g[0] = beta;
+    for (int i = 1; i <= m; ++i) g[i] = 0.0;
+    if (out_beta) *out_beta = beta;
+  }
+}
+
+template <typename T, typename TR>
+__global__ void k_scale_into(long long n, const TR* r, const GState* st, T* v0) {
+  const double beta = st->beta;
+  const double inv = beta > 0.0 ? 1.0 / beta : 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v0[i] = (T)((double)r[i] * inv);
+}
+
+__global__ void k_col_to_f32(long long n, const double* V, long long ld, const GState* st, float* out) {
+  if (st->done) return;
+  const double* v = V + (long long)st->j * ld;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)v[i];
+}
+__global__ void k_f32_to_col(long long n, const float* in, double* Z, long long ld, const GState* st) {
+  if (st->done) return;
+  double* z = Z + (long long)st->j * ld;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[i] = (double)in[i];
+}
+// inner solve runs only when the outer step is live
+__global__ void k_gate(const GState* outer, GState* inner) {
+  if (outer->done) inner->done = 1;
+}
+
+__global__ void k_bj_setup(int N, const int* diag, const double* A, const double* dD, double* Dinv, float* Dinv32,
+                           int* singular) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    double a[4][8];
+    const double* blk = A + 16ll * diag[n];
+    double scale = 0.0;
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        double v = blk[4 * r + c];
+        if (dD) v += dD[16ll * n + 4 * r + c];
+        a[r][c] = v;
+        a[r][4 + c] = (r == c) ? 1.0 : 0.0;
+        scale = fmax(scale, fabs(v));
+      }
+    bool ok = scale > 0.0;
+    for (int col = 0; col < 4 && ok; ++col) {
+      int piv = col;
+      for (int r = col + 1; r < 4; ++r)
+        if (fabs(a[r][col]) > fabs(a[piv][col])) piv = r;
+      if (!(fabs(a[piv][col]) > 1e-300 * scale + 0.0) || !(fabs(a[piv][col]) > 0.0)) { ok = false; break; }
+      if (piv != col)
+        for (int c = 0; c < 8; ++c) { double t = a[col][c]; a[col][c] = a[piv][c]; a[piv][c] = t; }
+      double inv = 1.0 / a[col][col];
+      for (int c = 0; c < 8; ++c) a[col][c] *= inv;
+      for (int r = 0; r < 4; ++r) {
+        if (r == col) continue;
+        double f = a[r][col];
+        if (f != 0.0)
+          for (int c = 0; c < 8; ++c) a[r][c] -= f * a[col][c];
+      }
+    }
+    if (!ok) atomicAdd(singular, 1);
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        double v = ok ? a[r][4 + c] : (r == c ? 1.0 : 0.0);
+        Dinv[16ll * n + 4 * r + c] = v;
+        if (Dinv32) Dinv32[16ll * n + 4 * r + c] = (float)v;
+      }
+  }
+}
+
+__global__ void k_to_f32(long long n, const double* in, float* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+int spmv_grid(int N) { return grid_for((long long)N * 32, 256, kSMs * 16); }
+int vec_grid(long long n) { return grid_for(n, 256, kSMs * 8); }
+
+}  // namespace
+
+Krylov::~Krylov() {
+  if (h_scal) cudaFreeHost(h_scal);
+}
+
+void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
+  GOAL_REQUIRE(m_ >= 1 && m_ < kMaxM && mi_ >= 1 && mi_ < kMaxM, GOAL_ERR_ARG, "krylov size must be in [1, 255]");
+  if (!h_scal) GOAL_CUDA(cudaMallocHost(&h_scal, 64 * sizeof(double)));
+  if (n_ != n || m_ != m) {
+    V.alloc((size_t)n_ * (m_ + 1));
+    Z.alloc((size_t)n_ * m_);
+    w.alloc(n_);
+    r.alloc(n_);
+    H.alloc((size_t)(m_ + 1) * m_);
+    cs.alloc(m_ + 1);
+    sn.alloc(m_ + 1);
+    g.alloc(m_ + 2);
+    y.alloc(m_ + 1);
+  }
+  red.alloc((size_t)(kMaxM + 4) * kSMs * 8);
+  scal.alloc(64);
+  flag.alloc(8);
+  if (mixed && (n_ != n || mi_ != mi || !V32.ptr)) {
+    V32.alloc((size_t)n_ * (mi_ + 1));
+    w32.alloc(n_);
+    r32.alloc(n_);
+  }
+  if (mixed) {
+    Hi.alloc((size_t)(mi_ + 1) * mi_);
+    csi.alloc(mi_ + 1);
+    sni.alloc(mi_ + 1);
+    gi.alloc(mi_ + 2);
+    yi.alloc(mi_ + 1);
+    if (A32.n != 16ull * nnzb) A32.alloc(16ll * nnzb);
+  }
+  dots.alloc(kMaxM + 2);
+  n = n_;
+  m = m_;
+  mi = mi_;
+}
+
+int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, Krylov& K) {
+  const int N = A.num_nodes;
+  K.Dinv.alloc(16ll * N);
+  K.Dinv32.alloc(16ll * N);
+  K.flag.alloc(8);
+  GOAL_CUDA(cudaMemsetAsync(K.flag.ptr, 0, sizeof(int), K.stream));
+  k_bj_setup<<<grid_for(N, 128), 128, 0, K.stream>>>(N, A.diag, vals, dD, K.Dinv.ptr, K.Dinv32.ptr, K.flag.ptr);
+  GOAL_CHECK_LAUNCH();
+  int sing = 0;
+  GOAL_CUDA(cudaMemcpyAsync(&sing, K.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, K.stream));
+  GOAL_CUDA(cudaStreamSynchronize(K.stream));
+  return sing;
+}
+
+void make_fp32_copy(const BsrView& A, const double* vals, Krylov& K) {
+  K.A32.alloc(16ll * A.nnzb);
+  k_to_f32<<<vec_grid(16ll * A.nnzb), 256, 0, K.stream>>>(16ll * A.nnzb, vals, K.A32.ptr);
+  GOAL_CHECK_LAUNCH();
+}
+
+void spmv64(const BsrView& A, const double* vals, const double* x, double* y, cudaStream_t s) {
+  k_spmv<double, false><<<spmv_grid(A.num_nodes), 256, 0, s>>>(A.num_nodes, A.brow_ptr, A.bcol, vals, x, nullptr, y);
+  GOAL_CHECK_LAUNCH();
+}
+void spmv32(const BsrView& A, const float* vals, const float* x, float* y, cudaStream_t s) {
+  k_spmv<float, false><<<spmv_grid(A.num_nodes), 256, 0, s>>>(A.num_nodes, A.brow_ptr, A.bcol, vals, x, nullptr, y);
+  GOAL_CHECK_LAUNCH();
+}
+
+namespace {
+
+// One Arnoldi step's orthogonalization (CGS with a conditional second pass),
+// normalization and Givens update, on state st.
+template <typename T>
+void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, double* cs, double* sn, double* g,
+                  double* dots, double* red, int jmax, double tol_abs, cudaStream_t s) {
+  const int nbx = vec_grid(n);
+  const int nchunks = (jmax + 2 + kDotChunk - 1) / kDotChunk;
+  double* part = red;
+  double* npart = red + (size_t)(kMaxM + 2) * nbx;
+  for (int pass = 0; pass < 2; ++pass) {
+    k_multidot<T><<<dim3(nbx, nchunks), 256, 0, s>>>(n, V, n, w, st, part, pass);
+    GOAL_CHECK_LAUNCH();
+    k_dots_fin<<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
+    GOAL_CHECK_LAUNCH();
+    k_update<T><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
+    GOAL_CHECK_LAUNCH();
+    k_norm_fin<<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
+    GOAL_CHECK_LAUNCH();
+  }
+  k_normalize<T><<<nbx, 256, 0, s>>>(n, V, n, w, st, H, ldh);
+  GOAL_CHECK_LAUNCH();
+  k_givens<<<1, 1, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
+  GOAL_CHECK_LAUNCH();
+}
+
+double read_norm(long long n, const double* x, Krylov& K) {
+  const int nbx = vec_grid(n);
+  k_norm2_part<double><<<nbx, 256, 0, K.stream>>>(n, x, K.red.ptr);
+  GOAL_CHECK_LAUNCH();
+  k_cycle_fin<<<1, 256, 0, K.stream>>>(nbx, K.red.ptr, reinterpret_cast<GState*>(K.scal.ptr + 16), K.scal.ptr + 40,
+                                       0, K.scal.ptr + 8);
+  GOAL_CHECK_LAUNCH();
+  GOAL_CUDA(cudaMemcpyAsync(K.h_scal, K.scal.ptr + 8, sizeof(double), cudaMemcpyDeviceToHost, K.stream));
+  GOAL_CUDA(cudaStreamSynchronize(K.stream));
+  return K.h_scal[0];
+}
+
+}  // namespace
+
+SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double* x, const SolveParams& p, Krylov& K) {
+  auto t0 = std::chrono::steady_clock::now();
+  SolveStats out;
+  const int N = A.num_nodes;
+  const long long n = 4ll * N;
+  const bool mixed = p.precision == PREC_MIXED;
+  const int m = p.krylov_size;
+  const int mi = std::max(1, p.inner_iters);
+  K.reserve((int)n, m, mi, mixed, A.nnzb);
+  cudaStream_t s = K.stream;
+  GOAL_REQUIRE(K.Dinv.ptr, GOAL_ERR_STATE, "fgmres: block-Jacobi preconditioner not set up");
+  if (mixed) GOAL_REQUIRE(K.A32.ptr, GOAL_ERR_STATE, "fgmres: FP32 matrix copy missing");
+
+  GState* st = reinterpret_cast<GState*>(K.scal.ptr);         // outer state
+  GState* sti = reinterpret_cast<GState*>(K.scal.ptr + 24);   // inner state
+  double* dots = K.dots.ptr;
+  double* Hin = mixed ? K.Hi.ptr : nullptr;
+  double* csin = mixed ? K.csi.ptr : nullptr;
+  double* snin = mixed ? K.sni.ptr : nullptr;
+  double* gin = mixed ? K.gi.ptr : nullptr;
+  double* yin = mixed ? K.yi.ptr : nullptr;
+
+  const double bnorm = read_norm(n, b, K);
+  const double tol_abs = p.tolerance * (bnorm > 0.0 ? bnorm : 1.0);
+  // r = b - A x
+  k_spmv<double, true><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, x, b, K.r.ptr);
+  GOAL_CHECK_LAUNCH();
+  out.spmv64++;
+  double beta = read_norm(n, K.r.ptr, K);
+  out.rel_res = bnorm > 0 ? beta / bnorm : beta;
+  const int nbx = vec_grid(n);
+  while (beta > tol_abs && out.iters < p.max_iters) {
+    // start a cycle: V_0 = r / beta
+    k_norm2_part<double><<<nbx, 256, 0, s>>>(n, K.r.ptr, K.red.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_cycle_fin<<<1, 256, 0, s>>>(nbx, K.red.ptr, st, K.g.ptr, m, nullptr);
+    GOAL_CHECK_LAUNCH();
+    k_scale_into<double, double><<<nbx, 256, 0, s>>>(n, K.r.ptr, st, K.V.ptr);
+    GOAL_CHECK_LAUNCH();
+    const int steps = std::min(m, p.max_iters - out.iters);
+    int done_steps = 0;
+    for (int step = 0; step < steps; ++step) {
+      if (!mixed) {
+        k_bj_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv.ptr, K.V.ptr, K.Z.ptr, n, st);
+        GOAL_CHECK_LAUNCH();
+      } else {
+        // inner FP32 GMRES on A32 with right block-Jacobi, fixed mi iterations:
+        // Z_j = M^-1 V32 y with V32 the inner basis started from V_j
+        k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.r32.ptr);
+        GOAL_CHECK_LAUNCH();
+        k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.red.ptr);
+        GOAL_CHECK_LAUNCH();
+        k_cycle_fin<<<1, 256, 0, s>>>(nbx, K.red.ptr, sti, gin, mi, nullptr);
+        GOAL_CHECK_LAUNCH();
+        k_gate<<<1, 1, 0, s>>>(st, sti);
+        GOAL_CHECK_LAUNCH();
+        k_scale_into<float, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V32.ptr);
+        GOAL_CHECK_LAUNCH();
+        for (int it = 0; it < mi; ++it) {
+          k_bj_colin<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V32.ptr, n, sti, K.r32.ptr);
+          GOAL_CHECK_LAUNCH();
+          // r32 = M^-1 v_it ; w32 = A32 r32 (ld 0 keeps the input at r32)
+          k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
+                                                         K.w32.ptr);
+          GOAL_CHECK_LAUNCH();
+          arnoldi_orth<float>(n, K.V32.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0, s);
+        }
+        k_backsolve<<<1, 1, 0, s>>>(sti, Hin, mi + 1, gin, yin);
+        GOAL_CHECK_LAUNCH();
+        k_combine<float, float><<<nbx, 256, 0, s>>>(n, K.V32.ptr, n, yin, sti, K.w32.ptr, 1);
+        GOAL_CHECK_LAUNCH();
+        k_bj<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.w32.ptr, K.r32.ptr);
+        GOAL_CHECK_LAUNCH();
+        k_f32_to_col<<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.Z.ptr, n, st);
+        GOAL_CHECK_LAUNCH();
+        out.inner_iters += mi;
+        out.spmv32 += mi;
+      }
+      k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
+      GOAL_CHECK_LAUNCH();
+      out.spmv64++;
+      arnoldi_orth<double>(n, K.V.ptr, K.w.ptr, st, K.H.ptr, m + 1, K.cs.ptr, K.sn.ptr, K.g.ptr, dots, K.red.ptr, m,
+                           tol_abs, s);
+      GOAL_CUDA(cudaMemcpyAsync(K.h_scal, K.scal.ptr, sizeof(GState), cudaMemcpyDeviceToHost, s));
+      GOAL_CUDA(cudaStreamSynchronize(s));
+      const GState* hs = reinterpret_cast<const GState*>(K.h_scal);
+      done_steps = hs->j;
+      if (hs->done) break;
+    }
+    out.iters += done_steps;
+    k_backsolve<<<1, 1, 0, s>>>(st, K.H.ptr, m + 1, K.g.ptr, K.y.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_combine<double, double><<<nbx, 256, 0, s>>>(n, K.Z.ptr, n, K.y.ptr, st, x, 0);
+    GOAL_CHECK_LAUNCH();
+    k_spmv<double, true><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, x, b, K.r.ptr);
+    GOAL_CHECK_LAUNCH();
+    out.spmv64++;
+    double nb = read_norm(n, K.r.ptr, K);
+    if (!(nb == nb)) throw Error(GOAL_ERR_SOLVER, "fgmres: non-finite residual");
+    if (done_steps == 0) { beta = nb; break; }  // breakdown without progress
+    beta = nb;
+  }
+  out.rel_res = bnorm > 0 ? beta / bnorm : beta;
+  out.converged = beta <= tol_abs ? 1 : 0;
+  out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return out;
+}
+
+}  // namespace goal

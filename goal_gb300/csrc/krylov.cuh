@@ -1,0 +1,80 @@
+// Krylov solves on the 4x4-block matrix: the GB300 replacement of goal::solve
+// (src/goal_linear_solve.cpp:53-90; Belos BlockGMRES + MueLu AMG there).
+//
+//   plain  : FGMRES(m) in FP64, right block-Jacobi preconditioner (4x4 node blocks)
+//   mixed  : FGMRES(m) in FP64 whose preconditioner is a fixed number of inner
+//            GMRES iterations in FP32 (FP32 matrix copy, FP32 block-Jacobi);
+//            the outer FP64 iteration refines to the requested tolerance
+//   learned: either of the above with the block-Jacobi blocks corrected by the
+//            mesh-graph network (falls back to plain block-Jacobi when the
+//            iteration count exceeds a cap)
+// Convergence is on the true (unpreconditioned) residual ||b - A x|| / ||b||,
+// which right preconditioning makes equal to the GMRES residual estimate.
+// Every iteration runs on the device (Arnoldi, classical Gram-Schmidt with a
+// conditional second pass, Givens rotations); the host reads one residual
+// estimate per outer iteration.
+#pragma once
+
+#include "common.cuh"
+
+namespace goal {
+
+struct BsrView {
+  int num_nodes;
+  int nnzb;
+  const int* brow_ptr;
+  const int* bcol;
+  const int* diag;
+};
+
+enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
+enum Precond : int { PRECOND_BJ = 0, PRECOND_LEARNED = 1 };
+
+struct SolveParams {
+  int krylov_size = 100;      // outer restart length ("krylov size")
+  int max_iters = 2000;       // outer iteration cap ("max iters")
+  double tolerance = 1e-10;   // relative residual ("tolerance")
+  int precision = PREC_FP64;
+  int inner_iters = 30;       // FP32 inner GMRES iterations per outer iteration (mixed)
+  int precond = PRECOND_BJ;
+  int learned_cap = 0;        // fall back to plain block-Jacobi after this many outer iterations (0 = no cap)
+};
+
+struct SolveStats {
+  int iters = 0;              // outer iterations
+  int inner_iters = 0;        // total inner (FP32) iterations
+  double rel_res = 0.0;       // true relative residual at exit
+  double seconds = 0.0;
+  int converged = 0;
+  int fell_back = 0;          // learned preconditioner replaced by plain block-Jacobi
+  long long spmv64 = 0, spmv32 = 0;
+};
+
+// Device buffers of one solver instance (sized on first use).
+struct Krylov {
+  cudaStream_t stream = nullptr;
+  int n = 0, m = 0, mi = 0;
+  DevBuf<double> V, Z, w, r, H, cs, sn, g, y, red, scal, dots;
+  DevBuf<double> Hi, csi, sni, gi, yi;   // inner (FP32 solve) Hessenberg and rotations
+  DevBuf<float> V32, w32, r32, A32;
+  DevBuf<double> Dinv;       // 16 x N inverse diagonal blocks (FP64)
+  DevBuf<float> Dinv32;
+  DevBuf<int> flag;
+  double* h_scal = nullptr;  // pinned host mirror of a few scalars
+  ~Krylov();
+  void reserve(int n_, int m_, int mi_, bool mixed, int nnzb);
+};
+
+// Inverts the 4x4 diagonal blocks of A (optionally plus a correction dD,
+// 16 x N, added before inversion). Returns the number of singular blocks.
+int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, Krylov& K);
+// FP32 copy of the matrix values for the mixed solve.
+void make_fp32_copy(const BsrView& A, const double* vals, Krylov& K);
+
+void spmv64(const BsrView& A, const double* vals, const double* x, double* y, cudaStream_t s);
+void spmv32(const BsrView& A, const float* vals, const float* x, float* y, cudaStream_t s);
+
+// Solves A x = b (x holds the initial guess). All pointers are device pointers.
+SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double* x, const SolveParams& p, Krylov& K);
+
+}  // namespace goal

@@ -163,6 +163,86 @@ int goal_set_jac_dbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t);
 /* set_tbcs (src/goal_tbcs.cpp:29-85); error_weights = 1 uses the z_diff weights */
 int goal_set_tbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t, int error_weights);
 
+/* ---------------------------------------------------------------- linear solve
+ * goal::solve(params, A, x, b, disc) (src/goal_linear_solve.cpp:72-90) with
+ * A = dRdu of the SolInfo. precision: 0 = FP64 FGMRES with block-Jacobi;
+ * 1 = FP64 FGMRES whose preconditioner is inner_iters FP32 GMRES iterations
+ * (FP32 matrix and block-Jacobi). precond: 0 = block-Jacobi, 1 = learned
+ * block-Jacobi correction (see goal_learned_*), falling back to plain
+ * block-Jacobi when the outer iterations exceed learned_cap.
+ * Convergence: ||b - A x||_2 <= tolerance ||b||_2. */
+typedef struct {
+  int krylov_size;
+  int max_iters;
+  double tolerance;
+  int precision;
+  int inner_iters;
+  int precond;
+  int learned_cap;
+} goal_solve_params;
+
+typedef struct {
+  int iters;
+  int inner_iters;
+  int converged;
+  int fell_back;
+  double rel_res;
+  double seconds;
+  long long spmv64;
+  long long spmv32;
+} goal_solve_stats;
+
+/* b and x are host arrays of num_dofs values; x holds the initial guess. */
+int goal_solve(goal_sol_info s, const goal_solve_params* params, const double* b, double* x, goal_solve_stats* stats);
+/* the same with device pointers (no copies) */
+int goal_solve_device(goal_sol_info s, const goal_solve_params* params, const double* b, double* x,
+                      goal_solve_stats* stats);
+
+/* ---------------------------------------------------------------- Newton
+ * Primal::solve (src/goal_primal.cpp:111-137): per iteration the Jacobian chain,
+ * traction and Dirichlet conditions, R *= -1, the linear solve, U += du, the
+ * residual chain with its conditions, and ||R||_2 < tolerance (absolute).
+ * Returns GOAL_ERR_NEWTON when max_iters is reached without convergence. */
+typedef struct {
+  int iters;
+  int converged;
+  int linear_iters;
+  int inner_iters;
+  double norms[32];
+  double seconds_assembly;
+  double seconds_solve;
+} goal_newton_stats;
+int goal_primal_solve(goal_mechanics m, goal_sol_info s, goal_bcs b, double t_now, double t_old, int max_iters,
+                      double tolerance, const goal_solve_params* lin, goal_newton_stats* stats);
+
+/* ---------------------------------------------------------------- nested adjoint + DWR
+ * NestedAdjoint (src/goal_nested_adjoint.cpp): build_data creates the uniformly
+ * refined discretization, its mechanics (child states = parent states) and
+ * linear objects; run refreshes the prolonged solution and states, assembles the
+ * transposed Jacobian and dM/du, solves dRdu^T z = dMdu, forms z_coarse (edge
+ * midpoint interpolant) and z_diff, the estimate eta = -R.z, localizes the
+ * error with the PU-DWR weights and returns the bound sum_v |e_u + e_p| and the
+ * element indicators (base mesh: sum over the 8 children). Boundary conditions
+ * are given on the nested discretization (goal_nested_adjoint_disc). */
+typedef struct goal_nested_adjoint_s* goal_nested_adjoint;
+typedef struct {
+  double eta;
+  double bound;
+  double qoi;
+  goal_solve_stats solve;
+  double seconds_adjoint;
+  double seconds_solve;
+  double seconds_localize;
+} goal_dwr_result;
+int goal_nested_adjoint_create(goal_mechanics base, goal_nested_adjoint* out);
+int goal_nested_adjoint_disc(goal_nested_adjoint a, goal_disc* nested);
+int goal_nested_adjoint_run(goal_nested_adjoint a, goal_bcs nested_bcs, int qoi, double rho, double t_now,
+                            double t_old, const goal_solve_params* params, goal_dwr_result* result,
+                            double* base_error, double* nested_error);
+/* z (4*num_nodes of the nested mesh) of the last run */
+int goal_nested_adjoint_get_z(goal_nested_adjoint a, double* z);
+int goal_nested_adjoint_destroy(goal_nested_adjoint a);
+
 #ifdef __cplusplus
 }
 #endif

@@ -651,6 +651,48 @@ int orc_assemble(const Args* a) {
   return status;
 }
 
+// The same Jacobian chain evaluated with all host threads: elements are
+// evaluated in parallel into per-element buffers, then scattered in element
+// order (same sums as orc_assemble). Used as the timed CPU baseline.
+int orc_assemble_parallel(const Args* a, int chunk) {
+  const Args& A = *a;
+  if (!A.fad || A.qoi != 0) return orc_assemble(a);
+  int status = 0;
+  std::vector<double> buf((size_t)chunk * 272);
+  for (int e0 = 0; e0 < A.num_elems; e0 += chunk) {
+    int ne = std::min(chunk, A.num_elems - e0);
+#pragma omp parallel for schedule(dynamic, 64) reduction(| : status)
+    for (int k = 0; k < ne; ++k) {
+      ElemOut<Dual> o;
+      status |= eval_element<Dual>(A, e0 + k, 0.0, 1.0, o);
+      double* b = buf.data() + (size_t)k * 272;
+      for (int n = 0; n < 4; ++n)
+        for (int q = 0; q < 4; ++q) {
+          const Dual& r = (q < 3) ? o.Ru[n][q] : o.Rp[n];
+          b[4 * n + q] = r.v;
+          for (int c = 0; c < 16; ++c) b[16 + 16 * (4 * n + q) + c] = r.d[c];
+        }
+    }
+    for (int k = 0; k < ne; ++k) {
+      const int* v = A.tets + 4 * (e0 + k);
+      const double* b = buf.data() + (size_t)k * 272;
+      int lids[16];
+      for (int n = 0; n < 4; ++n)
+        for (int q = 0; q < 4; ++q) lids[4 * n + q] = 4 * v[n] + q;
+      for (int r = 0; r < 16; ++r) {
+        if (A.R) A.R[lids[r]] += b[r];
+        if (A.vals)
+          for (int c = 0; c < 16; ++c) {
+            int kk = (A.mode == 1) ? find_col(A, lids[r], lids[c]) : find_col(A, lids[c], lids[r]);
+            if (kk >= 0) A.vals[kk] += b[16 + 16 * r + c];
+          }
+      }
+    }
+  }
+  if (A.status) *A.status = status;
+  return status;
+}
+
 // set_resid_dbcs / set_jac_dbcs for one boundary condition (src/goal_dbcs.cpp:39-99).
 // rows are dofs node*4+eq, vals the prescribed values; jac != 0 also replaces
 // the CSR row by the identity row and zeroes dMdu.

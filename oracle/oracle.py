@@ -78,6 +78,8 @@ def lib():
                                     ctypes.c_void_p, ctypes.c_void_p]
         L.orc_assemble.restype = ctypes.c_int
         L.orc_assemble.argtypes = [ctypes.POINTER(_Args)]
+        L.orc_assemble_parallel.restype = ctypes.c_int
+        L.orc_assemble_parallel.argtypes = [ctypes.POINTER(_Args), ctypes.c_int]
         L.orc_apply_dbc.restype = None
         L.orc_apply_dbc.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -170,7 +172,7 @@ def assemble(mesh, model: int, mats: List[Material], u: np.ndarray, p: np.ndarra
              qoi: int = QOI_NONE, rho: float = 0.0,
              graph: Optional[Tuple[np.ndarray, np.ndarray]] = None,
              R: Optional[np.ndarray] = None, vals: Optional[np.ndarray] = None, dMdu: Optional[np.ndarray] = None,
-             error_weights: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None):
+             error_weights: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None, threads: bool = False):
     """One assemble(E, SolInfo*) of a chain; accumulates into R / vals / dMdu.
     Returns (qoi value, number of plastic points)."""
     L = lib()
@@ -217,7 +219,10 @@ def assemble(mesh, model: int, mats: List[Material], u: np.ndarray, p: np.ndarra
     a.qoi_value = _p(q)
     a.num_plastic = _p(npl)
     a.status = _p(st)
-    L.orc_assemble(ctypes.byref(a))
+    if threads:
+        L.orc_assemble_parallel(ctypes.byref(a), 32768)
+    else:
+        L.orc_assemble(ctypes.byref(a))
     if st[0] != 0:
         raise RuntimeError("J2: return mapping failed")
     return float(q[0]), int(npl[0])

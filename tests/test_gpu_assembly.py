@@ -3,8 +3,11 @@
 Bars: DOF numbering and CSR graph bit-exact; residual, Jacobian and states
 within 1e-12 relative (vectors: to the vector's max magnitude; matrices: to
 each row's max magnitude); QoI values within 1e-12 relative; KS dMdu within
-1e-10 relative at plastic points (the reference's AD through the return map
-cancels by a factor ~3 mubar/K there, which the closed-form tangent avoids).
+1e-10 relative: the reference differentiates von Mises through the stress after
+the mixed pressure replacement (differences of diagonal entries that carry the
+pressure) and, at plastic points, through the return-map iterates (which cancel
+by a factor ~3 mubar/K); the closed-form derivative has neither cancellation,
+so the two differ by the oracle's own rounding, measured at 7e-12.
 """
 import numpy as np
 import pytest
@@ -154,7 +157,7 @@ def test_adjoint_chain(meshes, model, qoi):
     assert rel_vec(s.R, R) < RTOL
     assert rel_rows(s.dRdu_csr(), vals, g[0]) < RTOL
     assert abs(q - oq) <= RTOL * abs(oq)
-    tol = 1e-10 if (qoi == O.QOI_KS and model == O.J2) else RTOL
+    tol = 1e-10 if qoi == O.QOI_KS else RTOL
     assert rel_vec(s.dMdu, dM) < tol
 
 
