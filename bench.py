@@ -46,6 +46,7 @@ def _args():
     ap.add_argument("--n", type=int, default=40, help="hexes per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--adjoint-n", type=int, default=40, help="base mesh of the adjoint-solve leg (0: skip)")
     return ap.parse_args()
 
 
@@ -134,7 +135,7 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "-lms", "20"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -228,6 +229,43 @@ def run_reference(a):
     }
     print(json.dumps(line))
     return 0
+
+
+# ------------------------------------------------------------------ adjoint leg
+def adjoint_leg(n, api):
+    """Adjoint solve on the nested (uniformly refined) mesh after one J2 load
+    step of the stretched cube (u_x = 0.002 on x=1, u=0 on x=0): dRdu^T z = dM/du
+    with the KS von Mises functional (rho = 20), solved to 1e-10 relative
+    residual with plain FP64 block-Jacobi FGMRES and with FP32-inner / FP64-outer
+    FGMRES; seconds and iterations of each, and the DWR estimates they give."""
+    from goal_gb300.mesh import kuhn_cube
+    mesh = kuhn_cube(n)
+    d = api.Disc(mesh)
+    m = api.Mechanics(d, api.J2, [[MAT["E"], MAT["nu"], MAT["K"], MAT["Y"], MAT["c0"]]])
+    s = api.SolInfo(d)
+    dbcs = [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", "0.002*t")]
+    bcs = api.Bcs(d, dbcs, [])
+    t0 = time.perf_counter()
+    newton = api.primal_solve(m, s, bcs, 1.0, 0.0, 10, 1e-8,
+                              api.solve_params(tolerance=1e-10, precision=api.MIXED, inner_iters=30, max_iters=2000))
+    t_primal = time.perf_counter() - t0
+    na = api.NestedAdjoint(m, dbcs, [])
+    out = {"base_elements": mesh.num_elems, "nested_elements": na.disc.num_elems, "nested_dofs": na.disc.num_dofs,
+           "newton_iters": newton["iters"], "primal_seconds": t_primal, "qoi": "KS von Mises rho=20",
+           "tolerance": 1e-10}
+    runs = {"plain_fp64": api.solve_params(krylov_size=100, tolerance=1e-10, max_iters=20000),
+            "mixed": api.solve_params(krylov_size=30, tolerance=1e-10, max_iters=2000, precision=api.MIXED,
+                                      inner_iters=30)}
+    for name, prm in runs.items():
+        r = na.run(api.QOI_KS_VM, 20.0, 1.0, 0.0, prm)
+        out[name] = {"seconds": r["seconds_solve"], "iters": r["solve"]["iters"],
+                     "inner_iters": r["solve"]["inner_iters"], "converged": r["solve"]["converged"],
+                     "rel_res": r["solve"]["rel_res"], "eta": r["eta"], "bound": r["bound"]}
+    p, mx = out["plain_fp64"], out["mixed"]
+    out["speedup_mixed_vs_plain"] = p["seconds"] / mx["seconds"] if mx["seconds"] > 0 else None
+    out["eta_rel_diff"] = abs(mx["eta"] - p["eta"]) / max(abs(p["eta"]), 1e-300)
+    na.close()
+    return out
 
 
 # ------------------------------------------------------------------ GPU leg
@@ -349,6 +387,11 @@ def main():
                      "algorithmic_bytes_per_step": alg},
         "clocks": clk,
     }
+    if a.adjoint_n > 0:
+        try:
+            line["adjoint_solve"] = adjoint_leg(a.adjoint_n, api)
+        except Exception as exc:  # the assembly line stands on its own
+            line["adjoint_solve"] = {"error": str(exc)[:300]}
     if not a.no_cpu_baseline:
         rate, ne = cpu_assembly_rate(mesh, u, p, Fp_old, eqps_old, a.cpu_seconds, False)
         line["cpu_baseline"] = {"value": rate, "unit": "elem/s", "cores": 1, "kind": "port",

@@ -11,7 +11,7 @@ class Chain(ctypes.Structure):
     """goal_chain"""
     _fields_ = [("mode", ctypes.c_int), ("jacobian", ctypes.c_int), ("save_states", ctypes.c_int),
                 ("qoi", ctypes.c_int), ("rho", ctypes.c_double), ("error_chain", ctypes.c_int),
-                ("overwrite", ctypes.c_int)]
+                ("overwrite", ctypes.c_int), ("colored", ctypes.c_int)]
 
 
 class SolveParams(ctypes.Structure):

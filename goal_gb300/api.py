@@ -225,10 +225,11 @@ class SolInfo:
 
 
 def assemble(mech: Mechanics, sol_info: Optional[SolInfo], mode: int, jacobian: bool, save_states: bool,
-             qoi: int = QOI_NONE, rho: float = 0.0, error_chain: bool = False, overwrite: bool = True) -> float:
+             qoi: int = QOI_NONE, rho: float = 0.0, error_chain: bool = False, overwrite: bool = True,
+             colored: bool = False) -> float:
     """assemble(E, SolInfo*) for one evaluator chain; returns the QoI value."""
     c = Chain(mode=mode, jacobian=int(jacobian), save_states=int(save_states), qoi=qoi, rho=rho,
-              error_chain=int(error_chain), overwrite=int(overwrite))
+              error_chain=int(error_chain), overwrite=int(overwrite), colored=int(colored))
     q = ctypes.c_double(0.0)
     check(lib().goal_assemble(mech.h, sol_info.h if sol_info is not None else None, ctypes.byref(c), ctypes.byref(q)))
     return q.value

@@ -471,6 +471,7 @@ int goal_assemble(goal_mechanics m, goal_sol_info s, const goal_chain* chain, do
   c.rho = chain->rho;
   c.error_chain = chain->error_chain;
   c.overwrite = chain->overwrite;
+  c.colored = chain->colored;
   GOAL_ARG(c.mode >= 0 && c.mode <= 2 && c.qoi >= 0 && c.qoi <= 2, "goal_assemble: bad chain");
   ErrorWeights w;
   if (c.error_chain) {

@@ -218,6 +218,24 @@ __global__ void k_permute(int E, const int* perm, const int* tets, const int* el
   }
 }
 
+__global__ void k_contrib_keys(int E, const int* blk_s, const int* tets_s, int* bkeys, int* bvals, int* nkeys,
+                               int* nvals, int* bcnt, int* ncnt) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
+    for (int q = 0; q < 16; ++q) {
+      int k = blk_s[(long long)q * E + s];
+      bkeys[16ll * s + q] = k;
+      bvals[16ll * s + q] = 16 * s + q;
+      atomicAdd(&bcnt[k], 1);
+    }
+    for (int a = 0; a < 4; ++a) {
+      int n = tets_s[(long long)a * E + s];
+      nkeys[4ll * s + a] = n;
+      nvals[4ll * s + a] = 4 * s + a;
+      atomicAdd(&ncnt[n], 1);
+    }
+  }
+}
+
 template <typename T>
 void exclusive_scan(const T* in, T* out, int n, cudaStream_t s) {
   size_t bytes = 0;
@@ -366,6 +384,31 @@ void Disc::build() {
                                               h.ptr);
   GOAL_CHECK_LAUNCH();
   GOAL_CUDA(cudaStreamSynchronize(s));
+  {
+    // contribution lists (stable sorts keep the element order within a block / node)
+    DevBuf<int> bk, bv, nk, nv, bks, nks, bcnt, ncnt;
+    bk.alloc(16ll * E);
+    bv.alloc(16ll * E);
+    nk.alloc(4ll * E);
+    nv.alloc(4ll * E);
+    bcnt.alloc(nnzb + 1);
+    ncnt.alloc(N + 1);
+    bcnt.zero(s);
+    ncnt.zero(s);
+    k_contrib_keys<<<grid_for(E, 256), 256, 0, s>>>(E, blk.ptr, tets.ptr, bk.ptr, bv.ptr, nk.ptr, nv.ptr, bcnt.ptr,
+                                                     ncnt.ptr);
+    GOAL_CHECK_LAUNCH();
+    bptr.alloc(nnzb + 1);
+    nptr.alloc(N + 1);
+    exclusive_scan(bcnt.ptr, bptr.ptr, nnzb + 1, s);
+    exclusive_scan(ncnt.ptr, nptr.ptr, N + 1, s);
+    bks.alloc(16ll * E);
+    blist.alloc(16ll * E);
+    sort_pairs(bk.ptr, bks.ptr, bv.ptr, blist.ptr, 16 * E, bits_for(nnzb), s);
+    nks.alloc(4ll * E);
+    nlist.alloc(4ll * E);
+    sort_pairs(nk.ptr, nks.ptr, nv.ptr, nlist.ptr, 4 * E, bits_for(N), s);
+  }
 
   // node sets / side sets to the device
   for (auto& kv : node_sets) kv.second->dev.upload(kv.second->host.data(), kv.second->host.size(), s);

@@ -80,6 +80,11 @@ struct Disc {
   DevBuf<int> blk, brow_ptr, bcol, diag;
   DevBuf<unsigned> first;
   DevBuf<int> color;  // colour per element (colour order)
+  // contribution lists of the two-phase (element buffer + gather) assembly:
+  // block k of the matrix sums element blocks blist[bptr[k]..bptr[k+1]) with
+  // entries 16*s + (4a+b); node n sums element rows nlist[nptr[n]..nptr[n+1])
+  // with entries 4*s + a. Both are ordered by element, so sums are deterministic.
+  DevBuf<int> bptr, blist, nptr, nlist;
 
   std::map<std::string, std::unique_ptr<NodeSet>> node_sets;
   std::map<std::string, std::unique_ptr<SideSet>> side_sets;

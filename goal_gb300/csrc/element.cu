@@ -61,6 +61,9 @@ struct ElemArgs {
   const double* Zd;
   const double* Zc;
   int* status;
+  double* ebuf;    // two-phase mode: per element [R (16) | 16 blocks x 16] (stride estride)
+  double* dbuf;    // two-phase mode: per element dM/du (16)
+  int estride;
   int begin, end;
   int stab, save, overwrite, qoi;
   double rho, ks_max, ks_scale;
@@ -111,7 +114,9 @@ __device__ bool exp_traceless_sym(const double A[3][3], double out[3][3]) {
   return ok;
 }
 
-template <int MODEL, int MODE, bool JAC, bool ERR>
+// BUF: element outputs go to the per-element buffer (phase 1 of the two-phase
+// assembly) instead of being accumulated in place by one colour at a time.
+template <int MODEL, int MODE, bool JAC, bool ERR, bool BUF>
 __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   const int s = a.begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.end) return;
@@ -345,9 +350,15 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
         Rp[n] = ((pval / kappa) - dUdJ) * (zp * 0.25) * V + (a.stab ? tauJ * (0.25 * vhz + zc * wv[n]) * V : 0.0);
       }
     }
-    const unsigned fm = a.overwrite ? __ldg(a.d.first + s) : 0u;
+    if constexpr (BUF) {
+      double* eb = a.ebuf + (size_t)s * a.estride;
 #pragma unroll
-    for (int n = 0; n < 4; ++n) acc4(a.R + 4 * v[n], (fm >> (16 + n)) & 1u, Ru[n][0], Ru[n][1], Ru[n][2], Rp[n]);
+      for (int n = 0; n < 4; ++n) st4(eb + 4 * n, Ru[n][0], Ru[n][1], Ru[n][2], Rp[n]);
+    } else {
+      const unsigned fm = a.overwrite ? __ldg(a.d.first + s) : 0u;
+#pragma unroll
+      for (int n = 0; n < 4; ++n) acc4(a.R + 4 * v[n], (fm >> (16 + n)) & 1u, Ru[n][0], Ru[n][1], Ru[n][2], Rp[n]);
+    }
   }
 
   // ---------------------------------------------------------------- QoI
@@ -418,7 +429,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   }
   // dM/du (QoI derivative) for the u dofs; pressure dofs do not enter the QoIs
   if (a.qoi != QOI_NONE) {
-    const unsigned fm = a.overwrite ? __ldg(a.d.first + s) : 0u;
+    const unsigned fm = (!BUF && a.overwrite) ? __ldg(a.d.first + s) : 0u;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       double d[3];
@@ -431,7 +442,8 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
         for (int k = 0; k < 3; ++k)
           d[k] = c1 * (vq * qv[b][k] + vh * hv[b][k] + vn * nv[b][k] - gs * hv[b][k]);
       }
-      acc4(a.dMdu + 4 * v[b], (fm >> (16 + b)) & 1u, d[0], d[1], d[2], 0.0);
+      if constexpr (BUF) st4(a.dbuf + 16ll * s + 4 * b, d[0], d[1], d[2], 0.0);
+      else acc4(a.dMdu + 4 * v[b], (fm >> (16 + b)) & 1u, d[0], d[1], d[2], 0.0);
     }
   }
 
@@ -441,7 +453,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   const double tJV = tauJ * V;
   const double ppc = V / (16.0 * kappa);
   const double pu0 = V * ((J + Jinv) * 0.125);
-  const unsigned fm = a.overwrite ? __ldg(a.d.first + s) : 0u;
+  const unsigned fm = (!BUF && a.overwrite) ? __ldg(a.d.first + s) : 0u;
 #pragma unroll
   for (int ai = 0; ai < 4; ++ai) {
     double CG[3];  // C G_a
@@ -473,7 +485,11 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
         K[3][k] = t;
       }
       K[3][3] = ppc + (a.stab ? tJV * eab : 0.0);
-      if (MODE == MODE_PRIMAL) {
+      if constexpr (BUF) {
+        double* eb = a.ebuf + (size_t)s * a.estride + 16 + 16 * (4 * ai + b);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) st4(eb + 4 * r, K[r][0], K[r][1], K[r][2], K[r][3]);
+      } else if (MODE == MODE_PRIMAL) {
         const int q = 4 * ai + b;
         double* blk = a.A + 16ll * __ldg(a.d.blk + q * E + s);
         const bool f1 = (fm >> q) & 1u;
@@ -570,12 +586,12 @@ __global__ void k_fill_identity(int E, double* Fp) {
 }
 
 template <int MODEL, int MODE, bool JAC, bool ERR>
-void launch_colours(const Disc& d, ElemArgs args, cudaStream_t st) {
+void launch_colours(const Disc& d, ElemArgs args, cudaStream_t st, bool buffered) {
   const int block = 128;
-  if constexpr (MODE == MODE_NONE) {
+  if (MODE == MODE_NONE || buffered) {
     args.begin = 0;
     args.end = d.num_elems;
-    k_elem<MODEL, MODE, JAC, ERR><<<(d.num_elems + block - 1) / block, block, 0, st>>>(args);
+    k_elem<MODEL, MODE, JAC, ERR, true><<<(d.num_elems + block - 1) / block, block, 0, st>>>(args);
     GOAL_CHECK_LAUNCH();
   } else {
   for (int c = 0; c < d.num_colors; ++c) {
@@ -583,28 +599,76 @@ void launch_colours(const Disc& d, ElemArgs args, cudaStream_t st) {
     args.end = d.color_ptr[c + 1];
     int n = args.end - args.begin;
     if (n <= 0) continue;
-    k_elem<MODEL, MODE, JAC, ERR><<<(n + block - 1) / block, block, 0, st>>>(args);
+    k_elem<MODEL, MODE, JAC, ERR, false><<<(n + block - 1) / block, block, 0, st>>>(args);
     GOAL_CHECK_LAUNCH();
   }
   }
 }
 
 template <int MODEL>
-void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t st) {
+void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t st, bool buf) {
   if (c.error_chain) {
     GOAL_REQUIRE(!c.jacobian && c.mode == MODE_PRIMAL, GOAL_ERR_ARG, "the error chain is a residual (PRIMAL) chain");
-    launch_colours<MODEL, MODE_PRIMAL, false, true>(d, args, st);
+    launch_colours<MODEL, MODE_PRIMAL, false, true>(d, args, st, buf);
     return;
   }
   if (c.mode == MODE_NONE) {
-    if (c.jacobian) launch_colours<MODEL, MODE_NONE, true, false>(d, args, st);
-    else launch_colours<MODEL, MODE_NONE, false, false>(d, args, st);
+    if (c.jacobian) launch_colours<MODEL, MODE_NONE, true, false>(d, args, st, true);
+    else launch_colours<MODEL, MODE_NONE, false, false>(d, args, st, true);
   } else if (c.mode == MODE_PRIMAL) {
-    if (c.jacobian) launch_colours<MODEL, MODE_PRIMAL, true, false>(d, args, st);
-    else launch_colours<MODEL, MODE_PRIMAL, false, false>(d, args, st);
+    if (c.jacobian) launch_colours<MODEL, MODE_PRIMAL, true, false>(d, args, st, buf);
+    else launch_colours<MODEL, MODE_PRIMAL, false, false>(d, args, st, buf);
   } else {
     GOAL_REQUIRE(c.jacobian, GOAL_ERR_ARG, "ADJOINT mode is a Jacobian (FADT) chain");
-    launch_colours<MODEL, MODE_ADJOINT, true, false>(d, args, st);
+    launch_colours<MODEL, MODE_ADJOINT, true, false>(d, args, st, buf);
+  }
+}
+
+// Phase 2 of the two-phase assembly: every matrix block sums its element
+// blocks in element order (4 threads per block, one per row); TRANSPOSE
+// accumulates the element blocks transposed (ADJOINT mode stores dR/du^T).
+template <bool TRANSPOSE>
+__global__ void __launch_bounds__(256) k_gather_blocks(int nnzb, const int* __restrict__ bptr,
+                                                       const int* __restrict__ blist, const double* __restrict__ ebuf,
+                                                       int estride, double* __restrict__ A, int accumulate) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4ll * nnzb;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(t >> 2), r = (int)(t & 3);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (accumulate) ld4(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+    const int c1 = __ldg(bptr + k + 1);
+    for (int c = __ldg(bptr + k); c < c1; ++c) {
+      const int v = __ldg(blist + c);
+      const int s = v >> 4, lb = v & 15;
+      if (TRANSPOSE) {
+        const int lt = ((lb & 3) << 2) | (lb >> 2);
+        const double* p = ebuf + (size_t)s * estride + 16 + 16 * lt + r;
+        a0 += __ldg(p); a1 += __ldg(p + 4); a2 += __ldg(p + 8); a3 += __ldg(p + 12);
+      } else {
+        double x0, x1, x2, x3;
+        ld4(ebuf + (size_t)s * estride + 16 + 16 * lb + 4 * r, x0, x1, x2, x3);
+        a0 += x0; a1 += x1; a2 += x2; a3 += x3;
+      }
+    }
+    st4(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+  }
+}
+
+// Phase 2 for nodal vectors: node n, row q sums the element rows of its
+// incident elements (entries 4*s + a of nlist) in element order.
+__global__ void __launch_bounds__(256) k_gather_nodes(int N, const int* __restrict__ nptr,
+                                                      const int* __restrict__ nlist, const double* __restrict__ ebuf,
+                                                      int estride, double* __restrict__ out, int accumulate) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4ll * N;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(t >> 2), q = (int)(t & 3);
+    double acc = accumulate ? out[t] : 0.0;
+    const int c1 = __ldg(nptr + n + 1);
+    for (int c = __ldg(nptr + n); c < c1; ++c) {
+      const int v = __ldg(nlist + c);
+      acc += __ldg(ebuf + (size_t)(v >> 2) * estride + 4 * (v & 3) + q);
+    }
+    out[t] = acc;
   }
 }
 
@@ -731,12 +795,44 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
   a.ks_max = ks_max;
   a.ks_scale = ks_scale;
   GOAL_CUDA(cudaMemsetAsync(m.status.ptr, 0, sizeof(int), st));
-  if (c.overwrite && c.jacobian && c.qoi == QOI_NONE && s) {
+  if (c.overwrite && c.jacobian && c.qoi == QOI_NONE && s) {  // zero_all also clears dMdu
     // dMdu is not written by a chain without QoI: SolInfo::zero_all semantics
     GOAL_CUDA(cudaMemsetAsync(s->dMdu.ptr, 0, sizeof(double) * s->dMdu.n, st));
   }
-  if (m.model == MODEL_J2) dispatch<MODEL_J2>(d, c, a, st);
-  else dispatch<MODEL_NEOHOOKEAN>(d, c, a, st);
+  const bool buf = !c.colored && (c.mode != MODE_NONE || c.jacobian);
+  const bool scatter = c.mode != MODE_NONE;
+  if (buf) {
+    a.estride = c.jacobian ? 272 : 16;
+    size_t need = (size_t)d.num_elems * a.estride;
+    if (m.ebuf.n < need) m.ebuf.alloc(need);
+    a.ebuf = m.ebuf.ptr;
+    if (c.jacobian && c.qoi != QOI_NONE) {
+      if (m.dbuf.n < 16ull * d.num_elems) m.dbuf.alloc(16ull * d.num_elems);
+      a.dbuf = m.dbuf.ptr;
+    }
+  }
+  if (m.model == MODEL_J2) dispatch<MODEL_J2>(d, c, a, st, buf);
+  else dispatch<MODEL_NEOHOOKEAN>(d, c, a, st, buf);
+  if (buf && scatter) {
+    const int acc = c.overwrite ? 0 : 1;
+    k_gather_nodes<<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(d.num_nodes, d.nptr.ptr, d.nlist.ptr,
+                                                                        m.ebuf.ptr, a.estride, s->R.ptr, acc);
+    GOAL_CHECK_LAUNCH();
+    if (c.jacobian) {
+      if (c.mode == MODE_ADJOINT)
+        k_gather_blocks<true><<<grid_for(4ll * d.nnzb, 256), 256, 0, st>>>(d.nnzb, d.bptr.ptr, d.blist.ptr, m.ebuf.ptr,
+                                                                           a.estride, s->A.ptr, acc);
+      else
+        k_gather_blocks<false><<<grid_for(4ll * d.nnzb, 256), 256, 0, st>>>(d.nnzb, d.bptr.ptr, d.blist.ptr,
+                                                                            m.ebuf.ptr, a.estride, s->A.ptr, acc);
+      GOAL_CHECK_LAUNCH();
+    }
+  }
+  if (buf && c.jacobian && c.qoi != QOI_NONE && s) {
+    k_gather_nodes<<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(d.num_nodes, d.nptr.ptr, d.nlist.ptr, m.dbuf.ptr,
+                                                                        16, s->dMdu.ptr, c.overwrite ? 0 : 1);
+    GOAL_CHECK_LAUNCH();
+  }
   int hstat = 0;
   GOAL_CUDA(cudaMemcpyAsync(&hstat, m.status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
   double q = 0.0;

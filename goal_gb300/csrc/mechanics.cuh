@@ -33,6 +33,8 @@ struct Mechanics {
   DevBuf<double> U;         // 4N nodal solution: u_x u_y u_z p per node (the DOF layout)
   StatesDev st;
   DevBuf<double> qoi_elem;  // E   per-element QoI values (colour order)
+  DevBuf<double> ebuf;      // two-phase assembly: per-element R and 16 4x4 blocks (272 doubles)
+  DevBuf<double> dbuf;      // two-phase assembly: per-element dM/du (16 doubles)
   DevBuf<double> red;       // reduction scratch
   DevBuf<int> status;       // 1: return-map failures, non-finite etc.
   void init();
@@ -57,6 +59,7 @@ struct Chain {
   double rho = 0.0;
   int error_chain = 0;      // Mechanics::build_error weights (src/goal_mechanics.cpp:169-218)
   int overwrite = 1;        // outputs start from zero (fuses SolInfo::zero_*)
+  int colored = 0;          // 1: accumulate in place one colour at a time (no element buffer)
 };
 
 struct ErrorWeights {

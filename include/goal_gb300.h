@@ -139,7 +139,12 @@ int goal_sol_info_destroy(goal_sol_info s);
  *   Nested adjoint    {ADJOINT, jacobian 1, save 0, qoi} (src/goal_nested_adjoint.cpp:163-180)
  *   Error             {PRIMAL, jacobian 0, save 0, error_chain 1} (src/goal_nested_adjoint.cpp:217-234)
  * overwrite = 1 makes the assembly start its outputs from zero (the zero_*
- * calls that precede every assembly in goal); 0 accumulates into them. */
+ * calls that precede every assembly in goal); 0 accumulates into them.
+ * Both scatter strategies are deterministic and need no atomics: the default
+ * evaluates every element in one launch into a per-element buffer and then
+ * sums each matrix block / nodal row over its incident elements in element
+ * order; colored = 1 evaluates one colour (no two elements sharing a node) per
+ * launch and accumulates in place, without the buffer (2176 bytes per element). */
 typedef struct {
   int mode;
   int jacobian;
@@ -148,6 +153,7 @@ typedef struct {
   double rho;
   int error_chain;
   int overwrite;
+  int colored; /* 0: element buffer + deterministic gather (default); 1: colour-by-colour in place */
 } goal_chain;
 int goal_assemble(goal_mechanics m, goal_sol_info s, const goal_chain* chain, double* qoi_value);
 

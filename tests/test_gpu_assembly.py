@@ -101,12 +101,13 @@ def test_coloring_is_valid(meshes, name):
         assert len(np.unique(nodes)) == len(nodes), f"colour {c} shares nodes"
 
 
+@pytest.mark.parametrize("colored", [False, True])
 @pytest.mark.parametrize("model,u_scale", [(O.NEOHOOKEAN, 0.02), (O.J2, 2e-4), (O.J2, 2e-3)])
-def test_primal_jacobian_chain(meshes, model, u_scale):
+def test_primal_jacobian_chain(meshes, model, u_scale, colored):
     mesh = meshes["kuhn3"]
     u, p, st = random_state(mesh, 11, u_scale, model)
     d, m, s = make_gpu(mesh, model, u, p, st)
-    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=True)
+    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=True, colored=colored)
     g = O.csr_graph(mesh.num_nodes, mesh.tets)
     R = np.zeros(4 * mesh.num_nodes)
     vals = np.zeros(len(g[1]))
@@ -136,9 +137,10 @@ def test_residual_chain(meshes, model):
     assert rel_vec(m.get_state(api.SIGMA), ost.sigma) < RTOL
 
 
+@pytest.mark.parametrize("colored", [False, True])
 @pytest.mark.parametrize("model,qoi", [(O.NEOHOOKEAN, O.QOI_AVG_DISP), (O.NEOHOOKEAN, O.QOI_KS),
                                        (O.J2, O.QOI_AVG_DISP), (O.J2, O.QOI_KS)])
-def test_adjoint_chain(meshes, model, qoi):
+def test_adjoint_chain(meshes, model, qoi, colored):
     mesh = meshes["kuhn3"]
     u, p, st = random_state(mesh, 7, 0.02 if model == O.NEOHOOKEAN else 1e-3, model)
     # stored stresses that the KS pre-pass reads: the model's own stresses
@@ -147,7 +149,7 @@ def test_adjoint_chain(meshes, model, qoi):
     st.sigma[:] = ost0.sigma * 1.05
     d, m, s = make_gpu(mesh, model, u, p, st)
     rho = 20.0
-    q = api.assemble(m, s, api.ADJOINT, jacobian=True, save_states=False, qoi=qoi, rho=rho)
+    q = api.assemble(m, s, api.ADJOINT, jacobian=True, save_states=False, qoi=qoi, rho=rho, colored=colored)
     g = O.csr_graph(mesh.num_nodes, mesh.tets)
     R = np.zeros(4 * mesh.num_nodes)
     vals = np.zeros(len(g[1]))
@@ -242,14 +244,18 @@ def test_nested_mesh_matches_oracle(meshes, name):
     assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
 
 
-def test_assembly_is_deterministic_and_overwrite_matches_accumulate(meshes):
+@pytest.mark.parametrize("colored", [False, True])
+def test_assembly_is_deterministic_and_overwrite_matches_accumulate(meshes, colored):
     mesh = meshes["graded"]
     u, p, st = random_state(mesh, 19, 1e-3, O.J2)
     d, m, s = make_gpu(mesh, O.J2, u, p, st)
-    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False)
+    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, colored=colored)
     R1, A1 = s.R, s.dRdu_bsr()
-    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False)
+    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, colored=colored)
     assert np.array_equal(R1, s.R) and np.array_equal(A1, s.dRdu_bsr())
     s.zero_all()
-    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, overwrite=False)
+    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, overwrite=False, colored=colored)
     assert np.array_equal(R1, s.R) and np.array_equal(A1, s.dRdu_bsr())
+    # both scatter strategies assemble the same matrix (up to summation order)
+    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, colored=not colored)
+    assert np.abs(s.dRdu_bsr() - A1).max() <= 1e-13 * np.abs(A1).max()
