@@ -306,11 +306,18 @@ def primal_solve(mech: Mechanics, s: SolInfo, bcs: Bcs, t_now: float, t_old: flo
                  tolerance: float = 1e-8, params: Optional[SolveParams] = None) -> dict:
     """Primal::solve (Newton); raises GoalError(GOAL_ERR_NEWTON) when it fails."""
     st = NewtonStats()
-    check(lib().goal_primal_solve(mech.h, s.h, bcs.h, t_now, t_old, max_iters, tolerance,
-                                  ctypes.byref(params or solve_params()), ctypes.byref(st)))
-    return dict(iters=st.iters, converged=bool(st.converged), linear_iters=st.linear_iters,
-                inner_iters=st.inner_iters, norms=list(st.norms[:st.iters]),
-                seconds_assembly=st.seconds_assembly, seconds_solve=st.seconds_solve)
+    rc = lib().goal_primal_solve(mech.h, s.h, bcs.h, t_now, t_old, max_iters, tolerance,
+                                 ctypes.byref(params or solve_params()), ctypes.byref(st))
+    out = dict(iters=st.iters, converged=bool(st.converged), linear_iters=st.linear_iters,
+               inner_iters=st.inner_iters, norms=list(st.norms[:min(st.iters, 32)]),
+               seconds_assembly=st.seconds_assembly, seconds_solve=st.seconds_solve)
+    if rc != 0:
+        try:
+            check(rc)
+        except GoalError as e:
+            e.stats = out
+            raise
+    return out
 
 
 class NestedAdjoint:
@@ -358,6 +365,63 @@ class NestedAdjoint:
             self.bcs.close()
             self.disc.h = None  # owned by the nested adjoint
             lib().goal_nested_adjoint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Learned:
+    """The learned block-Jacobi correction (mesh-graph network, see goal_gb300.h)."""
+
+    def __init__(self, seed: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().goal_learned_create(seed, ctypes.byref(h)))
+        self.h = h
+        n = ctypes.c_int()
+        check(lib().goal_learned_num_params(self.h, ctypes.byref(n)))
+        self.num_params = n.value
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(lib().goal_learned_get_params(self.h, _ptr(out)))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().goal_learned_set_params(self.h, _ptr(p)))
+
+    def loss_grad(self, s: SolInfo, probes: Optional[np.ndarray] = None, num_probes: int = 4, seed: int = 0):
+        loss = ctypes.c_double()
+        grad = np.zeros(self.num_params, np.float32)
+        if probes is not None:
+            pr = np.ascontiguousarray(probes, dtype=np.float64)
+            num_probes = pr.shape[0]
+        else:
+            pr = None
+        check(lib().goal_learned_loss_grad(self.h, s.h, num_probes, _ptr(pr), seed, ctypes.byref(loss), _ptr(grad)))
+        return loss.value, grad
+
+    def corrections(self, s: SolInfo) -> np.ndarray:
+        C = np.zeros((s.disc.num_nodes, 16), np.float32)
+        check(lib().goal_learned_corrections(self.h, s.h, _ptr(C)))
+        return C
+
+    def train(self, systems, epochs: int = 50, lr: float = 1e-3, num_probes: int = 8, seed: int = 0) -> np.ndarray:
+        arr = (ctypes.c_void_p * len(systems))(*[x.h.value for x in systems])
+        losses = np.zeros(epochs)
+        check(lib().goal_learned_train(self.h, arr, len(systems), epochs, lr, num_probes, seed, _ptr(losses)))
+        return losses
+
+    def attach(self, s: SolInfo):
+        check(lib().goal_sol_info_set_learned(s.h, self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().goal_learned_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -7,6 +7,7 @@
 #include "../../include/goal_gb300.h"
 #include "capi_internal.cuh"
 #include "driver.cuh"
+#include "mpnn.cuh"
 
 namespace goal {
 
@@ -118,6 +119,13 @@ struct goal_bcs_s {
   Disc* d = nullptr;
   std::vector<DBC> dbcs;
   std::vector<TBC> tbcs;
+};
+struct goal_learned_s {
+  Mpnn net;
+  cudaStream_t stream = nullptr;
+  ~goal_learned_s() {
+    if (stream) cudaStreamDestroy(stream);
+  }
 };
 struct goal_nested_adjoint_s {
   NestedAdjoint a;
@@ -663,6 +671,107 @@ int goal_nested_adjoint_get_z(goal_nested_adjoint a, double* z) {
 int goal_nested_adjoint_destroy(goal_nested_adjoint a) {
   GOAL_API_BEGIN
   delete a;
+  GOAL_API_END
+}
+
+int goal_learned_create(int seed, goal_learned* out) {
+  GOAL_API_BEGIN
+  GOAL_ARG(out, "null argument");
+  auto h = std::make_unique<goal_learned_s>();
+  GOAL_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  h->net.stream = h->stream;
+  h->net.init(seed);
+  *out = h.release();
+  GOAL_API_END
+}
+
+int goal_learned_num_params(goal_learned l, int* n) {
+  GOAL_API_BEGIN
+  GOAL_ARG(l && n, "null argument");
+  *n = MpnnLayout::total;
+  GOAL_API_END
+}
+
+int goal_learned_get_params(goal_learned l, float* params) {
+  GOAL_API_BEGIN
+  GOAL_ARG(l && params, "null argument");
+  l->net.stream = l->stream;
+  l->net.download();
+  std::memcpy(params, l->net.host_params.data(), sizeof(float) * MpnnLayout::total);
+  GOAL_API_END
+}
+
+int goal_learned_set_params(goal_learned l, const float* params) {
+  GOAL_API_BEGIN
+  GOAL_ARG(l && params, "null argument");
+  l->net.stream = l->stream;
+  l->net.host_params.assign(params, params + MpnnLayout::total);
+  l->net.upload();
+  GOAL_API_END
+}
+
+static BsrMatrix matrix_of(goal_sol_info s) {
+  BsrMatrix M;
+  M.v = bsr_view(*s->s->disc);
+  M.vals = s->s->A.ptr;
+  return M;
+}
+
+int goal_learned_loss_grad(goal_learned l, goal_sol_info s, int num_probes, const double* probes, int seed,
+                           double* loss, float* grad) {
+  GOAL_API_BEGIN
+  GOAL_ARG(l && s && num_probes >= 1, "goal_learned_loss_grad: bad arguments");
+  l->net.stream = s->s->disc->stream;
+  DevBuf<double> pd;
+  if (probes) pd.upload(probes, (size_t)num_probes * 4 * s->s->disc->num_nodes, l->net.stream);
+  double L = mpnn_loss_grad(l->net, matrix_of(s), num_probes, probes ? pd.ptr : nullptr, (unsigned)seed);
+  if (loss) *loss = L;
+  if (grad) {
+    l->net.grad.download(grad, l->net.stream);
+    GOAL_CUDA(cudaStreamSynchronize(l->net.stream));
+  }
+  GOAL_API_END
+}
+
+int goal_learned_corrections(goal_learned l, goal_sol_info s, float* C) {
+  GOAL_API_BEGIN
+  GOAL_ARG(l && s && C, "null argument");
+  l->net.stream = s->s->disc->stream;
+  mpnn_forward(l->net, matrix_of(s), false);
+  GOAL_CUDA(cudaMemcpyAsync(C, l->net.C.ptr, sizeof(float) * 16 * s->s->disc->num_nodes, cudaMemcpyDeviceToHost,
+                            l->net.stream));
+  GOAL_CUDA(cudaStreamSynchronize(l->net.stream));
+  GOAL_API_END
+}
+
+int goal_learned_train(goal_learned l, const goal_sol_info* systems, int num_systems, int epochs, float lr,
+                       int num_probes, int seed, double* losses) {
+  GOAL_API_BEGIN
+  GOAL_ARG(l && systems && num_systems >= 1 && epochs >= 1 && num_probes >= 1, "goal_learned_train: bad arguments");
+  for (int e = 0; e < epochs; ++e) {
+    double sum = 0.0;
+    for (int k = 0; k < num_systems; ++k) {
+      goal_sol_info s = systems[k];
+      l->net.stream = s->s->disc->stream;
+      sum += mpnn_loss_grad(l->net, matrix_of(s), num_probes, nullptr, (unsigned)(seed + 131 * (e * num_systems + k)));
+      mpnn_adam(l->net, lr, 0.9f, 0.999f, 1e-8f);
+    }
+    if (losses) losses[e] = sum;
+  }
+  GOAL_CUDA(cudaStreamSynchronize(l->net.stream));
+  GOAL_API_END
+}
+
+int goal_sol_info_set_learned(goal_sol_info s, goal_learned l) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s, "null argument");
+  s->s->learned = l ? &l->net : nullptr;
+  GOAL_API_END
+}
+
+int goal_learned_destroy(goal_learned l) {
+  GOAL_API_BEGIN
+  delete l;
   GOAL_API_END
 }
 

@@ -2,6 +2,7 @@
 #include <chrono>
 
 #include "driver.cuh"
+#include "mpnn.cuh"
 
 namespace goal {
 
@@ -140,9 +141,31 @@ BsrView bsr_view(const Disc& d) {
 SolveStats linear_solve(SolInfo& s, const SolveParams& p, const double* b, double* x, Krylov& K, const double* dD) {
   K.stream = s.disc->stream;
   BsrView A = bsr_view(*s.disc);
+  if (p.precision == PREC_MIXED) make_fp32_copy(A, s.A.ptr, K);
+  if (p.precond == PRECOND_LEARNED) {
+    GOAL_REQUIRE(s.learned, GOAL_ERR_STATE, "learned preconditioner requested but no network is attached");
+    s.learned->stream = K.stream;
+    BsrMatrix M{A, s.A.ptr};
+    mpnn_apply_to_block_jacobi(*s.learned, M, K);
+    SolveParams q = p;
+    if (p.learned_cap > 0) q.max_iters = std::min(p.max_iters, p.learned_cap);
+    SolveStats r = fgmres(A, s.A.ptr, b, x, q, K);
+    if (r.converged || p.learned_cap <= 0 || p.max_iters <= q.max_iters) return r;
+    // fall back to plain block-Jacobi, continuing from the current iterate
+    block_jacobi_setup(A, s.A.ptr, nullptr, K);
+    SolveParams q2 = p;
+    q2.max_iters = p.max_iters - r.iters;
+    SolveStats r2 = fgmres(A, s.A.ptr, b, x, q2, K);
+    r2.iters += r.iters;
+    r2.inner_iters += r.inner_iters;
+    r2.spmv64 += r.spmv64;
+    r2.spmv32 += r.spmv32;
+    r2.seconds += r.seconds;
+    r2.fell_back = 1;
+    return r2;
+  }
   int sing = block_jacobi_setup(A, s.A.ptr, dD, K);
   (void)sing;  // singular blocks fall back to identity blocks
-  if (p.precision == PREC_MIXED) make_fp32_copy(A, s.A.ptr, K);
   return fgmres(A, s.A.ptr, b, x, p, K);
 }
 

@@ -44,8 +44,11 @@ struct Mechanics {
 
 // Linear objects of one discretization (LinearObj, src/goal_sol_info.hpp:12-16).
 // dRdu is stored as 4x4 blocks (BSR) on the disc's block graph.
+struct Mpnn;
+
 struct SolInfo {
   Disc* disc = nullptr;
+  Mpnn* learned = nullptr;  // network used when a solve asks for the learned preconditioner
   DevBuf<double> R, dMdu;   // 4N
   DevBuf<double> A;         // 16 x nnzb, block (n,m) row-major
   void init(Disc* d);

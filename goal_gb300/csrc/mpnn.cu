@@ -1,0 +1,679 @@
+// Forward, backward and Adam kernels of the learned block-Jacobi correction
+// (see mpnn.cuh). One warp per node; lane j owns hidden unit j. Layer weights
+// are staged in shared memory (rows padded to avoid bank conflicts) from the
+// bfloat16 copy; all arithmetic is float32. Weight gradients are summed per
+// warp, then over warps in a fixed order, so training is deterministic.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <random>
+
+#include "mpnn.cuh"
+
+namespace goal {
+
+namespace {
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kGridBlocks = kSMs;  // persistent grid for kernels with per-warp partials
+constexpr int kTotalWarps = kGridBlocks * kWarpsPerBlock;
+
+__device__ __forceinline__ float bf(unsigned short b) {
+  return __uint_as_float(((unsigned)b) << 16);
+}
+
+__device__ __forceinline__ unsigned hash32(unsigned x) {
+  x ^= x >> 16; x *= 0x7feb352du;
+  x ^= x >> 15; x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+__global__ void k_to_bf16(int n, const float* p, unsigned short* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    __nv_bfloat16 b = __float2bfloat16_rn(p[i]);
+    out[i] = *reinterpret_cast<unsigned short*>(&b);
+  }
+}
+
+// node features, scales and D^-1; x[16] holds log10 s until the mean is removed
+__global__ void k_features(int N, const int* brow_ptr, const int* bcol, const int* diag, const double* A, float* x,
+                           double* s, double* Dinv, int* deg) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    const double* D = A + 16ll * diag[n];
+    double smax = 0.0, dn = 0.0;
+    for (int q = 0; q < 16; ++q) { smax = fmax(smax, fabs(D[q])); dn += D[q] * D[q]; }
+    const double sc = smax > 0.0 ? smax : 1.0;
+    s[n] = sc;
+    for (int q = 0; q < 16; ++q) x[20ll * n + q] = (float)(D[q] / sc);
+    double offn = 0.0;
+    double offr[4] = {0, 0, 0, 0};
+    int nd = 0;
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      if (bcol[k] == n) continue;
+      ++nd;
+      double f = 0.0;
+      for (int q = 0; q < 16; ++q) {
+        double a = A[16ll * k + q];
+        f += a * a;
+        offr[q >> 2] += fabs(a);
+      }
+      offn += sqrt(f);
+    }
+    deg[n] = nd > 0 ? nd : 1;
+    dn = sqrt(dn);
+    x[20ll * n + 16] = (float)log10(sc);
+    x[20ll * n + 17] = (float)(offn / (dn > 0.0 ? dn : 1.0));
+    float flag = 0.0f;
+    for (int r = 0; r < 4; ++r) {
+      bool unit = true;
+      for (int c = 0; c < 4; ++c) unit = unit && (D[4 * r + c] == (r == c ? 1.0 : 0.0));
+      if (unit && offr[r] == 0.0) flag = 1.0f;
+    }
+    x[20ll * n + 18] = flag;
+    x[20ll * n + 19] = (float)((brow_ptr[n + 1] - brow_ptr[n] - 1) / 16.0);
+    // D^-1 (Gauss-Jordan with partial pivoting; identity for a singular block)
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) { a[r][c] = D[4 * r + c]; a[r][4 + c] = (r == c) ? 1.0 : 0.0; }
+    bool ok = smax > 0.0;
+    for (int col = 0; col < 4 && ok; ++col) {
+      int piv = col;
+      for (int r = col + 1; r < 4; ++r)
+        if (fabs(a[r][col]) > fabs(a[piv][col])) piv = r;
+      if (!(fabs(a[piv][col]) > 0.0)) { ok = false; break; }
+      if (piv != col)
+        for (int c = 0; c < 8; ++c) { double t = a[col][c]; a[col][c] = a[piv][c]; a[piv][c] = t; }
+      double inv = 1.0 / a[col][col];
+      for (int c = 0; c < 8; ++c) a[col][c] *= inv;
+      for (int r = 0; r < 4; ++r) {
+        if (r == col) continue;
+        double f = a[r][col];
+        if (f != 0.0)
+          for (int c = 0; c < 8; ++c) a[r][c] -= f * a[col][c];
+      }
+    }
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) Dinv[16ll * n + 4 * r + c] = ok ? a[r][4 + c] : (r == c ? 1.0 : 0.0);
+  }
+}
+
+__global__ void k_sum_log(int N, const float* x, double* part) {
+  KSum acc;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) acc.add((double)x[20ll * n + 16]);
+  acc = block_reduce(acc);
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = acc.s; part[2 * blockIdx.x + 1] = acc.c; }
+}
+__global__ void k_sub_log_mean(int N, int nb, const double* part, float* x) {
+  __shared__ double mean;
+  if (threadIdx.x == 0) {
+    KSum acc;
+    for (int i = 0; i < nb; ++i) {
+      KSum t;
+      t.s = part[2 * i];
+      t.c = part[2 * i + 1];
+      acc.add(t);
+    }
+    mean = acc.value() / N;
+  }
+  __syncthreads();
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
+    x[20ll * n + 16] = (float)((double)x[20ll * n + 16] - mean);
+}
+
+// index of block (m, n) for every block (n, m)
+__global__ void k_tmap(int N, const int* brow_ptr, const int* bcol, int* tmap) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      int m = bcol[k];
+      int lo = brow_ptr[m], hi = brow_ptr[m + 1];
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (bcol[mid] < n) lo = mid + 1;
+        else hi = mid;
+      }
+      tmap[k] = lo;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_encoder(int N, const unsigned short* w, const float* x, float* h) {
+  __shared__ float sW[kMH][kMF + 1];
+  __shared__ float sb[kMH];
+  for (int i = threadIdx.x; i < kMH * kMF; i += blockDim.x) sW[i / kMF][i % kMF] = bf(w[MpnnLayout::W0 + i]);
+  for (int i = threadIdx.x; i < kMH; i += blockDim.x) sb[i] = bf(w[MpnnLayout::b0 + i]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += (gridDim.x * blockDim.x) >> 5) {
+    float z = sb[lane];
+    for (int q = 0; q < kMF; ++q) z += sW[lane][q] * x[20ll * n + q];
+    h[32ll * n + lane] = fmaxf(z, 0.0f);
+  }
+}
+
+struct LayerSmem {
+  float We[kMH][kME + kMH + 1];
+  float be[kMH];
+  float Wu[kMH][2 * kMH + 1];
+  float bu[kMH];
+  float in[kWarpsPerBlock][kME + kMH];
+  float cat[kWarpsPerBlock][2 * kMH];
+  float d[kWarpsPerBlock][kMH];
+};
+
+__device__ void load_layer(LayerSmem& sm, const unsigned short* wl) {
+  for (int i = threadIdx.x; i < kMH * (kME + kMH); i += blockDim.x)
+    sm.We[i / (kME + kMH)][i % (kME + kMH)] = bf(wl[MpnnLayout::We + i]);
+  for (int i = threadIdx.x; i < kMH * 2 * kMH; i += blockDim.x) sm.Wu[i / (2 * kMH)][i % (2 * kMH)] = bf(wl[MpnnLayout::Wu + i]);
+  for (int i = threadIdx.x; i < kMH; i += blockDim.x) {
+    sm.be[i] = bf(wl[MpnnLayout::be + i]);
+    sm.bu[i] = bf(wl[MpnnLayout::bu + i]);
+  }
+  __syncthreads();
+}
+
+// stage [e_nm; h_m] of edge k in sm.in[w]
+__device__ __forceinline__ void stage_edge(LayerSmem& sm, int w, int lane, const double* A, long long k, double sn,
+                                           double smm, const float* h, int m) {
+  if (lane < kME) sm.in[w][lane] = (float)(A[16ll * k + lane] / sqrt(sn * smm));
+  sm.in[w][kME + lane] = h[32ll * m + lane];
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(256) k_layer_fwd(int N, const int* brow_ptr, const int* bcol, const double* A,
+                                                    const double* s, const int* deg, const unsigned short* wl,
+                                                    const float* h_in, float* h_out, float* tbuf, float* ubuf,
+                                                    float* aggbuf) {
+  __shared__ LayerSmem sm;
+  load_layer(sm, wl);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += (gridDim.x * blockDim.x) >> 5) {
+    const double sn = s[n];
+    float agg = 0.0f;
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      const int m = bcol[k];
+      if (m == n) continue;
+      stage_edge(sm, w, lane, A, k, sn, s[m], h_in, m);
+      float t = sm.be[lane];
+      for (int q = 0; q < kME + kMH; ++q) t += sm.We[lane][q] * sm.in[w][q];
+      if (tbuf) tbuf[32ll * k + lane] = t;
+      agg += fmaxf(t, 0.0f);
+      __syncwarp();
+    }
+    agg /= (float)deg[n];
+    const float hn = h_in[32ll * n + lane];
+    sm.cat[w][lane] = hn;
+    sm.cat[w][kMH + lane] = agg;
+    __syncwarp();
+    float u = sm.bu[lane];
+    for (int q = 0; q < 2 * kMH; ++q) u += sm.Wu[lane][q] * sm.cat[w][q];
+    if (ubuf) { ubuf[32ll * n + lane] = u; aggbuf[32ll * n + lane] = agg; }
+    h_out[32ll * n + lane] = hn + fmaxf(u, 0.0f);
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(256) k_decoder(int N, const unsigned short* w, const float* h, float* C) {
+  __shared__ float sW[16][kMH + 1];
+  __shared__ float sb[16];
+  for (int i = threadIdx.x; i < 16 * kMH; i += blockDim.x) sW[i / kMH][i % kMH] = bf(w[MpnnLayout::Wd + i]);
+  for (int i = threadIdx.x; i < 16; i += blockDim.x) sb[i] = bf(w[MpnnLayout::bd + i]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += (gridDim.x * blockDim.x) >> 5) {
+    if (lane < 16) {
+      float c = sb[lane];
+      for (int q = 0; q < kMH; ++q) c += sW[lane][q] * h[32ll * n + q];
+      C[16ll * n + lane] = c;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- loss
+__global__ void k_gauss(long long n, unsigned seed, double* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned a = hash32((unsigned)i * 2u + 1u + seed * 0x9e3779b9u);
+    unsigned b = hash32(a ^ (unsigned)(i >> 31) ^ 0x85ebca6bu);
+    double u1 = (a + 1.0) / 4294967297.0, u2 = b / 4294967296.0;
+    out[i] = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+  }
+}
+
+__global__ void k_bsr_mv(int N, const int* brow_ptr, const int* bcol, const double* A, const double* x, double* y,
+                         const double* sub) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 2, r = i & 3;
+    double acc = 0.0;
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      const double* a = A + 16ll * k + 4 * r;
+      const double* xx = x + 4ll * bcol[k];
+      acc += a[0] * xx[0] + a[1] * xx[1] + a[2] * xx[2] + a[3] * xx[3];
+    }
+    y[i] = sub ? sub[i] - acc : acc;
+  }
+}
+// y = A^T x using the transposed-block map
+__global__ void k_bsr_mv_t(int N, const int* brow_ptr, const int* bcol, const int* tmap, const double* A,
+                           const double* x, double* y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 2, c = i & 3;
+    double acc = 0.0;
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      const double* a = A + 16ll * tmap[k];  // block (m, n); entry (r, c) multiplies x_m[r]
+      const double* xx = x + 4ll * bcol[k];
+      acc += a[c] * xx[0] + a[4 + c] * xx[1] + a[8 + c] * xx[2] + a[12 + c] * xx[3];
+    }
+    y[i] = acc;
+  }
+}
+// y_n = (D^-1_n + C_n / s_n) v_n
+__global__ void k_apply_P(int N, const double* Dinv, const float* C, const double* s, const double* v, double* y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 2, r = i & 3;
+    double acc = 0.0;
+    for (int c = 0; c < 4; ++c) {
+      double p = Dinv[16ll * n + 4 * r + c] + (C ? (double)C[16ll * n + 4 * r + c] / s[n] : 0.0);
+      acc += p * v[4ll * n + c];
+    }
+    y[i] = acc;
+  }
+}
+__global__ void k_axpy(long long n, double a, const double* x, double* y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+__global__ void k_dot_part2(long long n, const double* a, const double* b, double* part) {
+  KSum acc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc.add(a[i] * b[i]);
+  acc = block_reduce(acc);
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = acc.s; part[2 * blockIdx.x + 1] = acc.c; }
+}
+__global__ void k_fin2(const double* part, int nb, double* out) {
+  KSum acc;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    KSum t;
+    t.s = part[2 * i];
+    t.c = part[2 * i + 1];
+    acc.add(t);
+  }
+  acc = block_reduce(acc);
+  if (threadIdx.x == 0) out[0] = acc.value();
+}
+// dP_n += coef g_n v_n^T with coef = -2 / |v|^2 ; loss += |r|^2 / |v|^2
+__global__ void k_dP(int N, const double* g, const double* v, const double* vv, double* dP) {
+  const double coef = -2.0 / vv[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 4, r = (i >> 2) & 3, c = i & 3;
+    dP[i] += coef * g[4ll * n + r] * v[4ll * n + c];
+  }
+}
+__global__ void k_dC(int N, const double* dP, const double* s, float* dC) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x)
+    dC[i] = (float)(dP[i] / s[i >> 4]);
+}
+
+// ---------------------------------------------------------------- backward
+// decoder: dh = Wd^T dC ; partial dWd, dbd per warp
+__global__ void __launch_bounds__(256) k_decoder_bwd(int N, const unsigned short* w, const float* h, const float* dC,
+                                                      float* dh, float* part, int P) {
+  __shared__ float sW[16][kMH + 1];
+  for (int i = threadIdx.x; i < 16 * kMH; i += blockDim.x) sW[i / kMH][i % kMH] = bf(w[MpnnLayout::Wd + i]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  float gW[16];
+  for (int j = 0; j < 16; ++j) gW[j] = 0.0f;
+  float gb = 0.0f;
+  for (int n = gw; n < N; n += (gridDim.x * blockDim.x) >> 5) {
+    const float hk = h[32ll * n + lane];
+    float acc = 0.0f;
+    for (int j = 0; j < 16; ++j) {
+      const float dc = dC[16ll * n + j];
+      acc += sW[j][lane] * dc;
+      gW[j] += dc * hk;
+    }
+    if (lane < 16) gb += dC[16ll * n + lane];
+    dh[32ll * n + lane] = acc;
+  }
+  float* p = part + (size_t)gw * P;
+  for (int j = 0; j < 16; ++j) p[MpnnLayout::Wd + j * kMH + lane] = gW[j];
+  if (lane < 16) p[MpnnLayout::bd + lane] = gb;
+}
+
+// node part of a layer's backward: du, dWu, dbu, dh_acc = dh + (Wu^T du)[:32], dagg = (Wu^T du)[32:]/deg
+__global__ void __launch_bounds__(256) k_layer_bwd_node(int N, const unsigned short* wl, int woff, const float* h_in,
+                                                         const float* ubuf, const float* aggbuf, const int* deg,
+                                                         const float* dh, float* dh_acc, float* dagg, float* part,
+                                                         int P) {
+  __shared__ LayerSmem sm;
+  load_layer(sm, wl);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  float gW[2 * kMH];
+  for (int q = 0; q < 2 * kMH; ++q) gW[q] = 0.0f;
+  float gb = 0.0f;
+  for (int n = gw; n < N; n += (gridDim.x * blockDim.x) >> 5) {
+    const float u = ubuf[32ll * n + lane];
+    const float du = (u > 0.0f) ? dh[32ll * n + lane] : 0.0f;
+    sm.cat[w][lane] = h_in[32ll * n + lane];
+    sm.cat[w][kMH + lane] = aggbuf[32ll * n + lane];
+    sm.d[w][lane] = du;
+    __syncwarp();
+    for (int q = 0; q < 2 * kMH; ++q) gW[q] += du * sm.cat[w][q];
+    gb += du;
+    float a0 = 0.0f, a1 = 0.0f;
+    for (int j = 0; j < kMH; ++j) {
+      a0 += sm.Wu[j][lane] * sm.d[w][j];
+      a1 += sm.Wu[j][kMH + lane] * sm.d[w][j];
+    }
+    dh_acc[32ll * n + lane] = dh[32ll * n + lane] + a0;
+    dagg[32ll * n + lane] = a1 / (float)deg[n];
+    __syncwarp();
+  }
+  float* p = part + (size_t)gw * P + woff;
+  for (int q = 0; q < 2 * kMH; ++q) p[MpnnLayout::Wu + lane * 2 * kMH + q] = gW[q];
+  p[MpnnLayout::bu + lane] = gb;
+}
+
+// edge part: dt, dWe, dbe and g_k = (We^T dt)[16:] for every edge k = (n, m)
+__global__ void __launch_bounds__(256) k_layer_bwd_edge(int N, const int* brow_ptr, const int* bcol, const double* A,
+                                                         const double* s, const unsigned short* wl, int woff,
+                                                         const float* h_in, const float* tbuf, const float* dagg,
+                                                         float* gbuf, float* part, int P) {
+  __shared__ LayerSmem sm;
+  load_layer(sm, wl);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  float gW[kME + kMH];
+  for (int q = 0; q < kME + kMH; ++q) gW[q] = 0.0f;
+  float gb = 0.0f;
+  for (int n = gw; n < N; n += (gridDim.x * blockDim.x) >> 5) {
+    const double sn = s[n];
+    const float da = dagg[32ll * n + lane];
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      const int m = bcol[k];
+      if (m == n) continue;
+      stage_edge(sm, w, lane, A, k, sn, s[m], h_in, m);
+      const float dt = (tbuf[32ll * k + lane] > 0.0f) ? da : 0.0f;
+      sm.d[w][lane] = dt;
+      __syncwarp();
+      for (int q = 0; q < kME + kMH; ++q) gW[q] += dt * sm.in[w][q];
+      gb += dt;
+      float g = 0.0f;
+      for (int j = 0; j < kMH; ++j) g += sm.We[j][kME + lane] * sm.d[w][j];
+      gbuf[32ll * k + lane] = g;
+      __syncwarp();
+    }
+  }
+  float* p = part + (size_t)gw * P + woff;
+  for (int q = 0; q < kME + kMH; ++q) p[MpnnLayout::We + lane * (kME + kMH) + q] = gW[q];
+  p[MpnnLayout::be + lane] = gb;
+}
+
+// dh_m = dh_acc_m + sum over edges (n, m) of g
+__global__ void k_layer_bwd_gather(int N, const int* brow_ptr, const int* bcol, const int* tmap, const float* dh_acc,
+                                   const float* gbuf, float* dh) {
+  const int lane = threadIdx.x & 31;
+  for (int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < N; m += (gridDim.x * blockDim.x) >> 5) {
+    float acc = dh_acc[32ll * m + lane];
+    for (int k = brow_ptr[m]; k < brow_ptr[m + 1]; ++k) {
+      if (bcol[k] == m) continue;
+      acc += gbuf[32ll * tmap[k] + lane];
+    }
+    dh[32ll * m + lane] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_encoder_bwd(int N, const float* x, const float* h0, const float* dh,
+                                                      float* part, int P) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  float gW[kMF];
+  for (int q = 0; q < kMF; ++q) gW[q] = 0.0f;
+  float gb = 0.0f;
+  for (int n = gw; n < N; n += (gridDim.x * blockDim.x) >> 5) {
+    const float dz = (h0[32ll * n + lane] > 0.0f) ? dh[32ll * n + lane] : 0.0f;
+    for (int q = 0; q < kMF; ++q) gW[q] += dz * x[20ll * n + q];
+    gb += dz;
+  }
+  float* p = part + (size_t)gw * P;
+  for (int q = 0; q < kMF; ++q) p[MpnnLayout::W0 + lane * kMF + q] = gW[q];
+  p[MpnnLayout::b0 + lane] = gb;
+}
+
+__global__ void k_sum_parts(int P, int nw, const float* part, float* grad) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+    float acc = 0.0f;
+    for (int w = 0; w < nw; ++w) acc += part[(size_t)w * P + i];
+    grad[i] = acc;
+  }
+}
+
+__global__ void k_adam(int n, float* p, const float* g, float* m1, float* m2, float lr, float b1, float b2, float eps,
+                       float c1, float c2, unsigned short* wbf) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float gi = g[i];
+    if (!(gi == gi)) gi = 0.0f;
+    m1[i] = b1 * m1[i] + (1.0f - b1) * gi;
+    m2[i] = b2 * m2[i] + (1.0f - b2) * gi * gi;
+    float mh = m1[i] / c1, vh = m2[i] / c2;
+    p[i] -= lr * mh / (sqrtf(vh) + eps);
+    __nv_bfloat16 b = __float2bfloat16_rn(p[i]);
+    wbf[i] = *reinterpret_cast<unsigned short*>(&b);
+  }
+}
+
+__global__ void k_write_bj(int N, const double* Dinv, const float* C, const double* s, double* out64, float* out32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) {
+    double v = Dinv[i] + (double)C[i] / s[i >> 4];
+    out64[i] = v;
+    out32[i] = (float)v;
+  }
+}
+
+}  // namespace
+
+void Mpnn::init(int seed) {
+  host_params.assign(MpnnLayout::total, 0.0f);
+  std::mt19937_64 rng((unsigned long long)seed);
+  std::normal_distribution<float> nd(0.0f, 1.0f);
+  auto fill = [&](int off, int rows, int cols) {
+    float sc = std::sqrt(2.0f / cols);
+    for (int i = 0; i < rows * cols; ++i) host_params[off + i] = nd(rng) * sc;
+  };
+  fill(MpnnLayout::W0, kMH, kMF);
+  for (int l = 0; l < kML; ++l) {
+    int o = MpnnLayout::L0 + l * MpnnLayout::layer;
+    fill(o + MpnnLayout::We, kMH, kME + kMH);
+    fill(o + MpnnLayout::Wu, kMH, 2 * kMH);
+  }
+  // decoder starts at zero: the untrained network is plain block-Jacobi
+  adam_t = 0;
+  upload();
+  m1.alloc(MpnnLayout::total);
+  m2.alloc(MpnnLayout::total);
+  m1.zero(stream);
+  m2.zero(stream);
+}
+
+void Mpnn::upload() {
+  params.upload(host_params.data(), host_params.size(), stream);
+  wbf.alloc(MpnnLayout::total);
+  k_to_bf16<<<grid_for(MpnnLayout::total, 256), 256, 0, stream>>>(MpnnLayout::total, params.ptr, wbf.ptr);
+  GOAL_CHECK_LAUNCH();
+  GOAL_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Mpnn::download() {
+  host_params.resize(MpnnLayout::total);
+  params.download(host_params.data(), stream);
+  GOAL_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Mpnn::reserve(int N, int nnzb) {
+  if (N > cap_nodes) {
+    x.alloc(20ll * N);
+    h.alloc(32ll * N * (kML + 1));
+    u.alloc(32ll * N * kML);
+    agg.alloc(32ll * N * kML);
+    C.alloc(16ll * N);
+    dC.alloc(16ll * N);
+    dh.alloc(32ll * N);
+    dagg.alloc(32ll * N);
+    s.alloc(N);
+    Dinv.alloc(16ll * N);
+    dP.alloc(16ll * N);
+    y.alloc(4ll * N);
+    r.alloc(4ll * N);
+    gT.alloc(4ll * N);
+    v.alloc(4ll * N);
+    deg.alloc(N);
+    cap_nodes = N;
+  }
+  if (nnzb > cap_blocks) {
+    t.alloc(32ll * nnzb * kML);
+    gbuf.alloc(32ll * nnzb);
+    tmap.alloc(nnzb);
+    cap_blocks = nnzb;
+  }
+  grad.alloc(MpnnLayout::total);
+  part.alloc((size_t)kTotalWarps * MpnnLayout::total);
+  red.alloc(2 * 2048 + 8);
+}
+
+void mpnn_forward(Mpnn& net, const BsrMatrix& A, bool keep) {
+  const int N = A.v.num_nodes;
+  cudaStream_t st = net.stream;
+  net.reserve(N, A.v.nnzb);
+  k_features<<<grid_for(N, 128), 128, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.v.diag, A.vals, net.x.ptr, net.s.ptr,
+                                               net.Dinv.ptr, net.deg.ptr);
+  GOAL_CHECK_LAUNCH();
+  const int nb = std::min(grid_for(N, 256), 1024);
+  k_sum_log<<<nb, 256, 0, st>>>(N, net.x.ptr, net.red.ptr);
+  GOAL_CHECK_LAUNCH();
+  k_sub_log_mean<<<grid_for(N, 256), 256, 0, st>>>(N, nb, net.red.ptr, net.x.ptr);
+  GOAL_CHECK_LAUNCH();
+  const int wgrid = grid_for((long long)N * 32, 256, kSMs * 8);
+  float* hbase = net.h.ptr;
+  k_encoder<<<wgrid, 256, 0, st>>>(N, net.wbf.ptr, net.x.ptr, hbase);
+  GOAL_CHECK_LAUNCH();
+  for (int l = 0; l < kML; ++l) {
+    const unsigned short* wl = net.wbf.ptr + MpnnLayout::L0 + l * MpnnLayout::layer;
+    float* hin = hbase + 32ll * N * l;
+    float* hout = hbase + 32ll * N * (l + 1);
+    k_layer_fwd<<<wgrid, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.s.ptr, net.deg.ptr, wl, hin, hout,
+                                       keep ? net.t.ptr + 32ll * A.v.nnzb * l : nullptr,
+                                       keep ? net.u.ptr + 32ll * N * l : nullptr,
+                                       keep ? net.agg.ptr + 32ll * N * l : nullptr);
+    GOAL_CHECK_LAUNCH();
+  }
+  k_decoder<<<wgrid, 256, 0, st>>>(N, net.wbf.ptr, hbase + 32ll * N * kML, net.C.ptr);
+  GOAL_CHECK_LAUNCH();
+}
+
+double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const double* probes_dev, unsigned seed) {
+  const int N = A.v.num_nodes;
+  const long long n = 4ll * N;
+  cudaStream_t st = net.stream;
+  mpnn_forward(net, A, true);
+  k_tmap<<<grid_for(N, 128), 128, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, net.tmap.ptr);
+  GOAL_CHECK_LAUNCH();
+  net.dP.zero(st);
+  const int vg = grid_for(n, 256);
+  const int nb = std::min(grid_for(n, 256), 1024);
+  double* scal = net.red.ptr + 2 * 1024 + 2;  // [vv, rr]
+  double loss = 0.0;
+  for (int p = 0; p < num_probes; ++p) {
+    if (probes_dev) {
+      GOAL_CUDA(cudaMemcpyAsync(net.v.ptr, probes_dev + (size_t)p * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    } else {
+      k_gauss<<<vg, 256, 0, st>>>(n, seed + 7919u * (unsigned)p, net.v.ptr);
+      GOAL_CHECK_LAUNCH();
+      if (p & 1) {  // smoothed probe: three damped block-Jacobi sweeps
+        for (int it = 0; it < 3; ++it) {
+          k_bsr_mv<<<vg, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.v.ptr, net.r.ptr, nullptr);
+          GOAL_CHECK_LAUNCH();
+          k_apply_P<<<vg, 256, 0, st>>>(N, net.Dinv.ptr, nullptr, net.s.ptr, net.r.ptr, net.y.ptr);
+          GOAL_CHECK_LAUNCH();
+          k_axpy<<<vg, 256, 0, st>>>(n, -0.6, net.y.ptr, net.v.ptr);
+          GOAL_CHECK_LAUNCH();
+        }
+      }
+    }
+    k_apply_P<<<vg, 256, 0, st>>>(N, net.Dinv.ptr, net.C.ptr, net.s.ptr, net.v.ptr, net.y.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_bsr_mv<<<vg, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.y.ptr, net.r.ptr, net.v.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_bsr_mv_t<<<vg, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, net.tmap.ptr, A.vals, net.r.ptr, net.gT.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_dot_part2<<<nb, 256, 0, st>>>(n, net.v.ptr, net.v.ptr, net.red.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_fin2<<<1, 1024, 0, st>>>(net.red.ptr, nb, scal);
+    GOAL_CHECK_LAUNCH();
+    k_dot_part2<<<nb, 256, 0, st>>>(n, net.r.ptr, net.r.ptr, net.red.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_fin2<<<1, 1024, 0, st>>>(net.red.ptr, nb, scal + 1);
+    GOAL_CHECK_LAUNCH();
+    k_dP<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.gT.ptr, net.v.ptr, scal, net.dP.ptr);
+    GOAL_CHECK_LAUNCH();
+    double hv[2];
+    GOAL_CUDA(cudaMemcpyAsync(hv, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GOAL_CUDA(cudaStreamSynchronize(st));
+    loss += hv[1] / hv[0];
+  }
+  k_dC<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.dP.ptr, net.s.ptr, net.dC.ptr);
+  GOAL_CHECK_LAUNCH();
+  // backward
+  const int P = MpnnLayout::total;
+  GOAL_CUDA(cudaMemsetAsync(net.part.ptr, 0, sizeof(float) * net.part.n, st));
+  float* hbase = net.h.ptr;
+  k_decoder_bwd<<<kGridBlocks, 256, 0, st>>>(N, net.wbf.ptr, hbase + 32ll * N * kML, net.dC.ptr, net.dh.ptr,
+                                              net.part.ptr, P);
+  GOAL_CHECK_LAUNCH();
+  DevBuf<float> dh_acc;
+  dh_acc.alloc(32ll * N);
+  for (int l = kML - 1; l >= 0; --l) {
+    const int woff = MpnnLayout::L0 + l * MpnnLayout::layer;
+    const unsigned short* wl = net.wbf.ptr + woff;
+    const float* hin = hbase + 32ll * N * l;
+    k_layer_bwd_node<<<kGridBlocks, 256, 0, st>>>(N, wl, woff, hin, net.u.ptr + 32ll * N * l,
+                                                   net.agg.ptr + 32ll * N * l, net.deg.ptr, net.dh.ptr, dh_acc.ptr,
+                                                   net.dagg.ptr, net.part.ptr, P);
+    GOAL_CHECK_LAUNCH();
+    k_layer_bwd_edge<<<kGridBlocks, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.s.ptr, wl, woff, hin,
+                                                   net.t.ptr + 32ll * A.v.nnzb * l, net.dagg.ptr, net.gbuf.ptr,
+                                                   net.part.ptr, P);
+    GOAL_CHECK_LAUNCH();
+    k_layer_bwd_gather<<<grid_for((long long)N * 32, 256, kSMs * 8), 256, 0, st>>>(
+        N, A.v.brow_ptr, A.v.bcol, net.tmap.ptr, dh_acc.ptr, net.gbuf.ptr, net.dh.ptr);
+    GOAL_CHECK_LAUNCH();
+  }
+  k_encoder_bwd<<<kGridBlocks, 256, 0, st>>>(N, net.x.ptr, hbase, net.dh.ptr, net.part.ptr, P);
+  GOAL_CHECK_LAUNCH();
+  k_sum_parts<<<grid_for(P, 256), 256, 0, st>>>(P, kTotalWarps, net.part.ptr, net.grad.ptr);
+  GOAL_CHECK_LAUNCH();
+  GOAL_CUDA(cudaStreamSynchronize(st));
+  return loss;
+}
+
+void mpnn_adam(Mpnn& net, float lr, float beta1, float beta2, float eps) {
+  net.adam_t += 1;
+  float c1 = 1.0f - std::pow(beta1, (float)net.adam_t);
+  float c2 = 1.0f - std::pow(beta2, (float)net.adam_t);
+  k_adam<<<grid_for(MpnnLayout::total, 256), 256, 0, net.stream>>>(MpnnLayout::total, net.params.ptr, net.grad.ptr,
+                                                                    net.m1.ptr, net.m2.ptr, lr, beta1, beta2, eps, c1,
+                                                                    c2, net.wbf.ptr);
+  GOAL_CHECK_LAUNCH();
+}
+
+void mpnn_apply_to_block_jacobi(Mpnn& net, const BsrMatrix& A, Krylov& K) {
+  const int N = A.v.num_nodes;
+  mpnn_forward(net, A, false);
+  K.Dinv.alloc(16ll * N);
+  K.Dinv32.alloc(16ll * N);
+  k_write_bj<<<grid_for(16ll * N, 256), 256, 0, net.stream>>>(N, net.Dinv.ptr, net.C.ptr, net.s.ptr, K.Dinv.ptr,
+                                                              K.Dinv32.ptr);
+  GOAL_CHECK_LAUNCH();
+}
+
+}  // namespace goal

@@ -249,6 +249,31 @@ int goal_nested_adjoint_run(goal_nested_adjoint a, goal_bcs nested_bcs, int qoi,
 int goal_nested_adjoint_get_z(goal_nested_adjoint a, double* z);
 int goal_nested_adjoint_destroy(goal_nested_adjoint a);
 
+/* ---------------------------------------------------------------- learned preconditioner
+ * A mesh-graph network (3 message-passing layers, width 32, bfloat16 weights,
+ * float32 arithmetic) that emits a correction C_n for every node's block of the
+ * block-Jacobi preconditioner: P_n = D_n^-1 + C_n / max|D_n|. It has no
+ * counterpart in the reference (goal preconditions with MueLu AMG,
+ * src/goal_linear_solve.cpp:59-65). Training minimizes sum_v |v - A P v|^2/|v|^2
+ * over probe vectors on the GPU with Adam. A solve with precond = 1 uses the
+ * network attached to the SolInfo. */
+typedef struct goal_learned_s* goal_learned;
+int goal_learned_create(int seed, goal_learned* out);
+int goal_learned_num_params(goal_learned l, int* n);
+int goal_learned_get_params(goal_learned l, float* params);
+int goal_learned_set_params(goal_learned l, const float* params);
+/* loss and gradient for the SolInfo's matrix; probes: num_probes x num_dofs host
+ * values, or NULL to draw them from seed (half of them smoothed) */
+int goal_learned_loss_grad(goal_learned l, goal_sol_info s, int num_probes, const double* probes, int seed,
+                           double* loss, float* grad);
+/* corrections C (16 per node, row-major 4x4) for the SolInfo's matrix */
+int goal_learned_corrections(goal_learned l, goal_sol_info s, float* C);
+/* epochs x (one Adam step per system); losses[epochs] = summed loss per epoch */
+int goal_learned_train(goal_learned l, const goal_sol_info* systems, int num_systems, int epochs, float lr,
+                       int num_probes, int seed, double* losses);
+int goal_sol_info_set_learned(goal_sol_info s, goal_learned l);
+int goal_learned_destroy(goal_learned l);
+
 #ifdef __cplusplus
 }
 #endif
