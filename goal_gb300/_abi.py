@@ -71,6 +71,8 @@ def _ctype(decl: str):
         return ctypes.c_longlong
     if base == "double":
         return ctypes.c_double
+    if base == "float":
+        return ctypes.c_float
     if base.startswith("goal_"):
         return ctypes.c_void_p  # opaque handle
     if base == "void":

@@ -33,6 +33,13 @@ def test_library_exports_every_declared_symbol():
     assert not missing, f"not exported: {missing}"
 
 
+def test_every_prototype_binds():
+    """ctypes prototypes for every declared function (no GPU work)."""
+    L = _lib()
+    for name in _abi.parse_header():
+        assert getattr(L, name).argtypes is not None
+
+
 def test_expression_kat_host():
     """test/control.cpp:12-15: sin(x)*cos(y) + 2*exp(t) - z at (1,2,3,4) within 1e-15."""
     L = _lib()
