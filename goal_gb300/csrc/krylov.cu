@@ -431,37 +431,43 @@ Krylov::~Krylov() {
   if (h_scal) cudaFreeHost(h_scal);
 }
 
+namespace {
+// grow-only: a buffer is reallocated only when it is smaller than required, so
+// one workspace can serve solves of any size (kernels index with the solve's n, m)
+template <typename T>
+void need(DevBuf<T>& b, size_t count) {
+  if (b.n < count || !b.ptr) b.alloc(count);
+}
+}  // namespace
+
 void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
   GOAL_REQUIRE(m_ >= 1 && m_ < kMaxM && mi_ >= 1 && mi_ < kMaxM, GOAL_ERR_ARG, "krylov size must be in [1, 255]");
   if (!h_scal) GOAL_CUDA(cudaMallocHost(&h_scal, 64 * sizeof(double)));
-  if (n_ != n || m_ != m) {
-    V.alloc((size_t)n_ * (m_ + 1));
-    Z.alloc((size_t)n_ * m_);
-    w.alloc(n_);
-    r.alloc(n_);
-    H.alloc((size_t)(m_ + 1) * m_);
-    cs.alloc(m_ + 1);
-    sn.alloc(m_ + 1);
-    g.alloc(m_ + 2);
-    y.alloc(m_ + 1);
-  }
-  red.alloc((size_t)(kMaxM + 4) * kSMs * 8);
-  scal.alloc(64);
-  flag.alloc(8);
-  if (mixed && (n_ != n || mi_ != mi || !V32.ptr)) {
-    V32.alloc((size_t)n_ * (mi_ + 1));
-    w32.alloc(n_);
-    r32.alloc(n_);
-  }
+  const size_t nn = (size_t)n_;
+  need(V, nn * (m_ + 1));
+  need(Z, nn * m_);
+  need(w, nn);
+  need(r, nn);
+  need(H, (size_t)(m_ + 1) * m_);
+  need(cs, m_ + 1);
+  need(sn, m_ + 1);
+  need(g, m_ + 2);
+  need(y, m_ + 1);
+  need(red, (size_t)(kMaxM + 4) * kSMs * 8);
+  need(scal, 64);
+  need(flag, 8);
+  need(dots, kMaxM + 2);
   if (mixed) {
-    Hi.alloc((size_t)(mi_ + 1) * mi_);
-    csi.alloc(mi_ + 1);
-    sni.alloc(mi_ + 1);
-    gi.alloc(mi_ + 2);
-    yi.alloc(mi_ + 1);
-    if (A32.n != 16ull * nnzb) A32.alloc(16ll * nnzb);
+    need(V32, nn * (mi_ + 1));
+    need(w32, nn);
+    need(r32, nn);
+    need(Hi, (size_t)(mi_ + 1) * mi_);
+    need(csi, mi_ + 1);
+    need(sni, mi_ + 1);
+    need(gi, mi_ + 2);
+    need(yi, mi_ + 1);
+    need(A32, 16ull * nnzb);
   }
-  dots.alloc(kMaxM + 2);
   n = n_;
   m = m_;
   mi = mi_;
@@ -469,9 +475,9 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
 
 int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, Krylov& K) {
   const int N = A.num_nodes;
-  K.Dinv.alloc(16ll * N);
-  K.Dinv32.alloc(16ll * N);
-  K.flag.alloc(8);
+  need(K.Dinv, 16ull * N);
+  need(K.Dinv32, 16ull * N);
+  need(K.flag, 8);
   GOAL_CUDA(cudaMemsetAsync(K.flag.ptr, 0, sizeof(int), K.stream));
   k_bj_setup<<<grid_for(N, 128), 128, 0, K.stream>>>(N, A.diag, vals, dD, K.Dinv.ptr, K.Dinv32.ptr, K.flag.ptr);
   GOAL_CHECK_LAUNCH();
@@ -482,7 +488,7 @@ int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, K
 }
 
 void make_fp32_copy(const BsrView& A, const double* vals, Krylov& K) {
-  K.A32.alloc(16ll * A.nnzb);
+  need(K.A32, 16ull * A.nnzb);
   k_to_f32<<<vec_grid(16ll * A.nnzb), 256, 0, K.stream>>>(16ll * A.nnzb, vals, K.A32.ptr);
   GOAL_CHECK_LAUNCH();
 }

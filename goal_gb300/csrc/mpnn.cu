@@ -669,8 +669,8 @@ void mpnn_adam(Mpnn& net, float lr, float beta1, float beta2, float eps) {
 void mpnn_apply_to_block_jacobi(Mpnn& net, const BsrMatrix& A, Krylov& K) {
   const int N = A.v.num_nodes;
   mpnn_forward(net, A, false);
-  K.Dinv.alloc(16ll * N);
-  K.Dinv32.alloc(16ll * N);
+  if (K.Dinv.n < 16ull * N) K.Dinv.alloc(16ll * N);
+  if (K.Dinv32.n < 16ull * N) K.Dinv32.alloc(16ll * N);
   k_write_bj<<<grid_for(16ll * N, 256), 256, 0, net.stream>>>(N, net.Dinv.ptr, net.C.ptr, net.s.ptr, K.Dinv.ptr,
                                                               K.Dinv32.ptr);
   GOAL_CHECK_LAUNCH();
