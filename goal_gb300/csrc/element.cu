@@ -87,6 +87,12 @@ __device__ __forceinline__ void acc4(double* p, bool first, double a, double b, 
   st4(p, a, b, c, d);
 }
 
+constexpr int kMatStride = 8;  // kappa, mu, K, Y, c0, 1/kappa, c0/(2 mu), 1/(16 kappa)
+constexpr double kThird = 1.0 / 3.0;
+
+// 1/(k+1) for the exponential series
+__constant__ double c_inv_k[80];
+
 // exp(A) for a symmetric traceless 3x3 A (A = dgam N) by the power series
 // reduced with Cayley-Hamilton: A^3 = I2 A + I3 I, I2 = tr(A^2)/2, I3 = det A.
 // Returns false if the series did not settle in 80 terms.
@@ -103,7 +109,7 @@ __device__ bool exp_traceless_sym(const double A[3][3], double out[3][3]) {
   bool ok = false;
   for (int k = 2; k < 80; ++k) {
     double nx = z * I3, ny = x + z * I2, nz = y;
-    double inv = 1.0 / (k + 1);
+    const double inv = c_inv_k[k];
     x = nx * inv; y = ny * inv; z = nz * inv;
     s0 += x; s1 += y; s2 += z;
     double mag = fabs(x) + fabs(y) + fabs(z);
@@ -130,11 +136,14 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   for (int q = 0; q < 12; ++q) G[q / 3][q % 3] = __ldg(a.d.grads + q * E + s);
   const double V = __ldg(a.d.vol + s);
   const int es = __ldg(a.d.elem_set + s);
-  const double kappa = __ldg(a.mats + 5 * es + 0);
-  const double mu = __ldg(a.mats + 5 * es + 1);
-  const double Kh = __ldg(a.mats + 5 * es + 2);
-  const double Yld = __ldg(a.mats + 5 * es + 3);
-  const double c0 = __ldg(a.mats + 5 * es + 4);
+  const double* mrow = a.mats + kMatStride * es;
+  const double kappa = __ldg(mrow + 0);
+  const double mu = __ldg(mrow + 1);
+  const double Kh = __ldg(mrow + 2);
+  const double Yld = __ldg(mrow + 3);
+  const double inv_kappa = __ldg(mrow + 5);   // 1 / kappa
+  const double tau_coef = __ldg(mrow + 6);    // c0 / (2 mu)
+  const double pp_coef = __ldg(mrow + 7);     // 1 / (16 kappa)
 
   // gather + interpolation (Displacement/Pressure at_point)
   double un[4][3], pn[4];
@@ -151,9 +160,6 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       t += un[3][i] * G[3][j];
       F[i][j] = t;
     }
-  double uval[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) uval[i] = ((un[0][i] * 0.25 + un[1][i] * 0.25) + un[2][i] * 0.25) + un[3][i] * 0.25;
   F[0][0] += 1.0; F[1][1] += 1.0; F[2][2] += 1.0;
   const double pval = ((pn[0] * 0.25 + pn[1] * 0.25) + pn[2] * 0.25) + pn[3] * 0.25;
   double gp[3];
@@ -181,17 +187,21 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
 
   // right Cauchy-Green of the plastic part (identity for neo-Hookean)
   double C[6] = {1.0, 1.0, 1.0, 0.0, 0.0, 0.0};  // xx yy zz xy yz xz
-  if (MODEL == MODEL_J2) {
+  double FC[3][3];  // F C
+  if constexpr (MODEL == MODEL_J2) {
 #pragma unroll
     for (int q = 0; q < 6; ++q) C[q] = __ldg(a.Cpinv + q * E + s);
-  }
-  // FC = F C
-  double FC[3][3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    FC[i][0] = F[i][0] * C[0] + F[i][1] * C[3] + F[i][2] * C[5];
-    FC[i][1] = F[i][0] * C[3] + F[i][1] * C[1] + F[i][2] * C[4];
-    FC[i][2] = F[i][0] * C[5] + F[i][1] * C[4] + F[i][2] * C[2];
+    for (int i = 0; i < 3; ++i) {
+      FC[i][0] = F[i][0] * C[0] + F[i][1] * C[3] + F[i][2] * C[5];
+      FC[i][1] = F[i][0] * C[3] + F[i][1] * C[1] + F[i][2] * C[4];
+      FC[i][2] = F[i][0] * C[5] + F[i][1] * C[4] + F[i][2] * C[2];
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) FC[i][j] = F[i][j];
   }
   // B = F C F^T (symmetric)
   double B00 = FC[0][0] * F[0][0] + FC[0][1] * F[0][1] + FC[0][2] * F[0][2];
@@ -203,7 +213,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   const double Ic = B00 + B11 + B22;
   const double Jm13 = rcbrt(J);
   const double alpha = mu * (Jm13 * Jm13);
-  const double Ic3 = Ic / 3.0;
+  const double Ic3 = Ic * kThird;
   // trial deviatoric Kirchhoff stress s = alpha dev(B)
   const double s00 = alpha * (B00 - Ic3), s11 = alpha * (B11 - Ic3), s22 = alpha * (B22 - Ic3);
   const double s01 = alpha * B01, s12 = alpha * B12, s02 = alpha * B02;
@@ -228,7 +238,8 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       double alpha1 = eq_old + sq23 * X1;
       double R1 = smag - (2.0 * mubar * X1 + sq23 * (Yld + Kh * alpha1));
       double r1 = fabs(R1);
-      bool conv1 = (r1 < 1.0e-11) || (r1 / Yld < 1.0e-11) || (r1 / fyield < 1.0e-11);
+      // goal's tests |R| < 1e-11, |R|/Y < 1e-11, |R|/f < 1e-11 (Y, f > 0)
+      bool conv1 = (r1 < 1.0e-11) || (r1 < 1.0e-11 * Yld) || (r1 < 1.0e-11 * fyield);
       kh = conv1 ? 0.0 : (2.0 / 3.0) * Kh;
       cc = 2.0 * mubar + kh;
       Xr = conv1 ? X1 : fyield / cc;
@@ -265,7 +276,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   sg[1][2] = sg[2][1] = s12 * gJ;
   sg[0][2] = sg[2][0] = s02 * gJ;
   {
-    double pbar = ((sg[0][0] + sg[1][1]) + sg[2][2]) / 3.0;
+    double pbar = ((sg[0][0] + sg[1][1]) + sg[2][2]) * kThird;
     double dp = pval - pbar;
     sg[0][0] += dp; sg[1][1] += dp; sg[2][2] += dp;
   }
@@ -290,7 +301,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   double tau = 0.0;
   if (a.stab) {
     const double hh = __ldg(a.d.h + s);
-    tau = 0.5 * c0 * hh * hh / mu;
+    tau = tau_coef * (hh * hh);
   }
   const double tauJ = tau * J;
   const double dUdJ = 0.5 * (J - Jinv);
@@ -306,7 +317,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       for (int n = 0; n < 4; ++n) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) Ru[n][i] = V * (T[i][0] * hv[n][0] + T[i][1] * hv[n][1] + T[i][2] * hv[n][2]);
-        Rp[n] = ((pval / kappa) - dUdJ) * 0.25 * V + (a.stab ? tauJ * wv[n] * V : 0.0);
+        Rp[n] = ((pval * inv_kappa) - dUdJ) * 0.25 * V + (a.stab ? tauJ * wv[n] * V : 0.0);
       }
     } else {
       // DWR weights: z_diff phi_a (momentum, pressure), z_coarse phi_a (stabilization)
@@ -347,7 +358,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
           double PGa = T[i][0] * hv[n][0] + T[i][1] * hv[n][1] + T[i][2] * hv[n][2];
           Ru[n][i] = V * (0.25 * Pg[i] + z[i] * PGa);
         }
-        Rp[n] = ((pval / kappa) - dUdJ) * (zp * 0.25) * V + (a.stab ? tauJ * (0.25 * vhz + zc * wv[n]) * V : 0.0);
+        Rp[n] = ((pval * inv_kappa) - dUdJ) * (zp * 0.25) * V + (a.stab ? tauJ * (0.25 * vhz + zc * wv[n]) * V : 0.0);
       }
     }
     if constexpr (BUF) {
@@ -364,11 +375,14 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   // ---------------------------------------------------------------- QoI
   double ks_w = 0.0;
   if (a.qoi == QOI_AVG_DISP) {
+    double uval[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) uval[i] = ((un[0][i] * 0.25 + un[1][i] * 0.25) + un[2][i] * 0.25) + un[3][i] * 0.25;
     double ev = 0.0;
     ev += uval[0] * V;
     ev += uval[1] * V;
     ev += uval[2] * V;
-    a.qoi_elem[s] = ev / 3.0;
+    a.qoi_elem[s] = ev * kThird;
   } else if (a.qoi == QOI_KS_VM) {
     double d1 = sg[0][0] - sg[1][1], d2 = sg[1][1] - sg[2][2], d3 = sg[2][2] - sg[0][0];
     double s7 = 0.5 * (d1 * d1 + d2 * d2 + d3 * d3 + 6.0 * (sg[0][1] * sg[0][1] + sg[1][2] * sg[1][2] + sg[2][0] * sg[2][0]));
@@ -434,7 +448,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
     for (int b = 0; b < 4; ++b) {
       double d[3];
       if (a.qoi == QOI_AVG_DISP) {
-        d[0] = d[1] = d[2] = V / 12.0;
+        d[0] = d[1] = d[2] = V * (1.0 / 12.0);
       } else {
         const double c1 = ks_w * 1.22474487139158904909 * Jinv;  // sqrt(3/2)/J
         const double gs = gamma * smag;
@@ -451,16 +465,21 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   const double gaV = ga * V;
   const double upf = V * J * 0.25;
   const double tJV = tauJ * V;
-  const double ppc = V / (16.0 * kappa);
+  const double ppc = V * pp_coef;
   const double pu0 = V * ((J + Jinv) * 0.125);
   const unsigned fm = (!BUF && a.overwrite) ? __ldg(a.d.first + s) : 0u;
 #pragma unroll
   for (int ai = 0; ai < 4; ++ai) {
     double CG[3];  // C G_a
-    CG[0] = C[0] * G[ai][0] + C[3] * G[ai][1] + C[5] * G[ai][2];
-    CG[1] = C[3] * G[ai][0] + C[1] * G[ai][1] + C[4] * G[ai][2];
-    CG[2] = C[5] * G[ai][0] + C[4] * G[ai][1] + C[2] * G[ai][2];
+    if constexpr (MODEL == MODEL_J2) {
+      CG[0] = C[0] * G[ai][0] + C[3] * G[ai][1] + C[5] * G[ai][2];
+      CG[1] = C[3] * G[ai][0] + C[1] * G[ai][1] + C[4] * G[ai][2];
+      CG[2] = C[5] * G[ai][0] + C[4] * G[ai][1] + C[2] * G[ai][2];
+    } else {
+      CG[0] = G[ai][0]; CG[1] = G[ai][1]; CG[2] = G[ai][2];
+    }
     const double Za0 = zs * hv[ai][0], Za1 = zs * hv[ai][1], Za2 = zs * hv[ai][2];
+    const double up0 = upf * hv[ai][0], up1 = upf * hv[ai][1], up2 = upf * hv[ai][2];
     const double pu1 = (a.stab ? tJV * wv[ai] : 0.0) - pu0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
@@ -476,7 +495,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
           if (i == k) t += cab;
           K[i][k] = t;
         }
-        K[i][3] = upf * hv[ai][i];
+        K[i][3] = (i == 0) ? up0 : ((i == 1) ? up1 : up2);
       }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -693,7 +712,14 @@ void Mechanics::init() {
   for (const MaterialRow& r : mats_h) {
     double kappa = r.E / (3.0 * (1.0 - 2.0 * r.nu));
     double mu = r.E / (2.0 * (1.0 + r.nu));
-    m.insert(m.end(), {kappa, mu, r.K, r.Y, r.c0});
+    m.insert(m.end(), {kappa, mu, r.K, r.Y, r.c0, 1.0 / kappa, 0.5 * r.c0 / mu, 1.0 / (16.0 * kappa)});
+  }
+  static bool table_ready = false;
+  if (!table_ready) {
+    double t[80];
+    for (int k = 0; k < 80; ++k) t[k] = 1.0 / (k + 1);
+    GOAL_CUDA(cudaMemcpyToSymbol(c_inv_k, t, sizeof(t)));
+    table_ready = true;
   }
   mats.upload(m.data(), m.size(), disc->stream);
   U.alloc(4ll * N);

@@ -417,6 +417,28 @@ __global__ void k_bj_setup(int N, const int* diag, const double* A, const double
   }
 }
 
+// Rows that are identity rows of the matrix (Dirichlet rows: the diagonal
+// block's row r is e_r and every other block's row r is zero) take their value
+// from b before the iteration starts. Block-Jacobi keeps those entries of every
+// Krylov vector at zero, so GMRES then works on the interior problem only
+// (without this the scale-1 Dirichlet rows of a Newton right-hand side stall
+// right-preconditioned GMRES against the stiffness-scaled interior rows).
+__global__ void k_lift_identity_rows(int N, const int* brow_ptr, const int* bcol, const int* diag, const double* A,
+                                     const double* b, double* x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    const int n = i >> 2, r = i & 3;
+    bool ident = true;
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1] && ident; ++k) {
+      const double* row = A + 16ll * k + 4 * r;
+      for (int c = 0; c < 4; ++c) {
+        const double want = (k == diag[n] && c == r) ? 1.0 : 0.0;
+        if (row[c] != want) { ident = false; break; }
+      }
+    }
+    if (ident) x[i] = b[i];
+  }
+}
+
 __global__ void k_to_f32(long long n, const double* in, float* out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = (float)in[i];
@@ -567,6 +589,8 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
 
   const double bnorm = read_norm(n, b, K);
   const double tol_abs = p.tolerance * (bnorm > 0.0 ? bnorm : 1.0);
+  k_lift_identity_rows<<<grid_for(n, 256), 256, 0, s>>>(N, A.brow_ptr, A.bcol, A.diag, vals, b, x);
+  GOAL_CHECK_LAUNCH();
   // r = b - A x
   k_spmv<double, true><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, x, b, K.r.ptr);
   GOAL_CHECK_LAUNCH();

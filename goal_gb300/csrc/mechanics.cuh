@@ -29,7 +29,7 @@ struct Mechanics {
   int model = MODEL_NEOHOOKEAN;
   bool stabilization = true;
   std::vector<MaterialRow> mats_h;
-  DevBuf<double> mats;      // per set: kappa, mu, K, Y, c0
+  DevBuf<double> mats;      // per set: kappa, mu, K, Y, c0, 1/kappa, c0/(2 mu), 1/(16 kappa)
   DevBuf<double> U;         // 4N nodal solution: u_x u_y u_z p per node (the DOF layout)
   StatesDev st;
   DevBuf<double> qoi_elem;  // E   per-element QoI values (colour order)
