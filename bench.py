@@ -232,38 +232,83 @@ def run_reference(a):
 
 
 # ------------------------------------------------------------------ adjoint leg
-def adjoint_leg(n, api):
-    """Adjoint solve on the nested (uniformly refined) mesh after one J2 load
-    step of the stretched cube (u_x = 0.002 on x=1, u=0 on x=0): dRdu^T z = dM/du
-    with the KS von Mises functional (rho = 20), solved to 1e-10 relative
-    residual with plain FP64 block-Jacobi FGMRES and with FP32-inner / FP64-outer
-    FGMRES; seconds and iterations of each, and the DWR estimates they give."""
+def _j2_step(api, n, steps, max_newton=15):
+    """``steps`` J2 load steps of the stretched cube (u = 0 on x=0, u_x = 0.001 t
+    on x=1 at t = 1, 2, ...), the states updated between steps. One step of
+    0.002 is past what full Newton from zero converges in (the plastic front
+    jumps); two steps of 0.001 converge in a few iterations each."""
     from goal_gb300.mesh import kuhn_cube
     mesh = kuhn_cube(n)
     d = api.Disc(mesh)
     m = api.Mechanics(d, api.J2, [[MAT["E"], MAT["nu"], MAT["K"], MAT["Y"], MAT["c0"]]])
     s = api.SolInfo(d)
-    dbcs = [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", "0.002*t")]
+    dbcs = [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", "0.001*t")]
     bcs = api.Bcs(d, dbcs, [])
+    iters = []
+    for k in range(1, steps + 1):
+        if k > 1:
+            m.update_states()
+        newton = api.primal_solve(m, s, bcs, float(k), float(k - 1), max_newton, 1e-8,
+                                  api.solve_params(tolerance=1e-10, precision=api.MIXED, inner_iters=30,
+                                                   krylov_size=30, max_iters=3000))
+        iters.append(newton["iters"])
+    return mesh, d, m, s, bcs, dbcs, {"iters": iters, "time": float(steps)}
+
+
+def train_learned(api, epochs=60):
+    """Training data the method produces: Newton Jacobians of J2 load steps at
+    three load levels and the transposed Jacobian of a nested adjoint."""
+    keep, systems = [], []
+    for steps in (1, 2, 3):
+        mesh, d, m, s, bcs, dbcs, _ = _j2_step(api, 10, steps)
+        api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False)
+        api.set_jac_dbcs(m, s, bcs, float(steps))
+        keep.append((d, m, s, bcs))
+        systems.append(s)
+    mesh, d, m, s, bcs, dbcs, _ = _j2_step(api, 6, 2)
+    na = api.NestedAdjoint(m, dbcs, [])
+    na.run(api.QOI_KS_VM, 20.0, 2.0, 1.0, api.solve_params(tolerance=1e-6, max_iters=50))
+    keep.append((d, m, s, bcs, na))
+    net = api.Learned(seed=0)
     t0 = time.perf_counter()
-    newton = api.primal_solve(m, s, bcs, 1.0, 0.0, 10, 1e-8,
-                              api.solve_params(tolerance=1e-10, precision=api.MIXED, inner_iters=30, max_iters=2000))
+    losses = net.train(systems, epochs=epochs, lr=2e-3, num_probes=8)
+    return net, keep, {"systems": len(systems), "epochs": epochs, "seconds": time.perf_counter() - t0,
+                       "loss_first": float(losses[0]), "loss_last": float(losses[-1])}
+
+
+def adjoint_leg(n, api):
+    """Adjoint solve on the nested (uniformly refined) mesh after two J2 load
+    steps of the stretched cube (u_x = 0.001 t on x=1, t = 1, 2; u=0 on x=0): dRdu^T z = dM/du
+    with the KS von Mises functional (rho = 20), to 1e-10 relative residual with
+    plain FP64 block-Jacobi FGMRES, with FP32-inner / FP64-outer FGMRES, and with
+    the learned block-Jacobi correction inside the mixed solver; seconds and
+    iterations of each and the DWR estimates they give."""
+    t0 = time.perf_counter()
+    mesh, d, m, s, bcs, dbcs, newton = _j2_step(api, n, 2)
     t_primal = time.perf_counter() - t0
+    net, keep, train = train_learned(api)
     na = api.NestedAdjoint(m, dbcs, [])
     out = {"base_elements": mesh.num_elems, "nested_elements": na.disc.num_elems, "nested_dofs": na.disc.num_dofs,
            "newton_iters": newton["iters"], "primal_seconds": t_primal, "qoi": "KS von Mises rho=20",
-           "tolerance": 1e-10}
-    runs = {"plain_fp64": api.solve_params(krylov_size=100, tolerance=1e-10, max_iters=20000),
-            "mixed": api.solve_params(krylov_size=30, tolerance=1e-10, max_iters=2000, precision=api.MIXED,
-                                      inner_iters=30)}
+           "tolerance": 1e-10, "training": train}
+    runs = {"plain_fp64": api.solve_params(krylov_size=100, tolerance=1e-10, max_iters=30000),
+            "mixed": api.solve_params(krylov_size=30, tolerance=1e-10, max_iters=3000, precision=api.MIXED,
+                                      inner_iters=30),
+            "learned_mixed": api.solve_params(krylov_size=30, tolerance=1e-10, max_iters=3000, precision=api.MIXED,
+                                              inner_iters=30, precond=api.PRECOND_LEARNED, learned_cap=1500)}
     for name, prm in runs.items():
-        r = na.run(api.QOI_KS_VM, 20.0, 1.0, 0.0, prm)
+        if name == "learned_mixed":
+            net.attach(na.si_handle())
+        r = na.run(api.QOI_KS_VM, 20.0, 2.0, 1.0, prm)
         out[name] = {"seconds": r["seconds_solve"], "iters": r["solve"]["iters"],
                      "inner_iters": r["solve"]["inner_iters"], "converged": r["solve"]["converged"],
-                     "rel_res": r["solve"]["rel_res"], "eta": r["eta"], "bound": r["bound"]}
-    p, mx = out["plain_fp64"], out["mixed"]
-    out["speedup_mixed_vs_plain"] = p["seconds"] / mx["seconds"] if mx["seconds"] > 0 else None
-    out["eta_rel_diff"] = abs(mx["eta"] - p["eta"]) / max(abs(p["eta"]), 1e-300)
+                     "fell_back": r["solve"]["fell_back"], "rel_res": r["solve"]["rel_res"], "eta": r["eta"],
+                     "bound": r["bound"]}
+    p = out["plain_fp64"]
+    for k in ("mixed", "learned_mixed"):
+        q = out[k]
+        out[f"speedup_{k}_vs_plain"] = p["seconds"] / q["seconds"] if q["seconds"] > 0 else None
+        out[f"eta_rel_diff_{k}"] = abs(q["eta"] - p["eta"]) / max(abs(p["eta"]), 1e-300)
     na.close()
     return out
 

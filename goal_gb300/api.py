@@ -355,6 +355,16 @@ class NestedAdjoint:
             out["nested_error"] = ne
         return out
 
+    def si_handle(self) -> "SolInfo":
+        """The nested linear objects (a non-owning SolInfo view)."""
+        sh = ctypes.c_void_p()
+        check(lib().goal_nested_adjoint_sol_info(self.h, ctypes.byref(sh)))
+        view = SolInfo.__new__(SolInfo)
+        view.disc = self.disc
+        view.h = sh
+        view.close = lambda: None
+        return view
+
     def z(self) -> np.ndarray:
         z = np.zeros(self.disc.num_dofs)
         check(lib().goal_nested_adjoint_get_z(self.h, _ptr(z)))

@@ -129,8 +129,12 @@ struct goal_learned_s {
 };
 struct goal_nested_adjoint_s {
   NestedAdjoint a;
-  goal_disc_s disc_view;  // non-owning view handed to goal_nested_adjoint_disc
-  ~goal_nested_adjoint_s() { disc_view.d.release(); }
+  goal_disc_s disc_view;      // non-owning views handed to goal_nested_adjoint_disc / _sol_info
+  goal_sol_info_s si_view;
+  ~goal_nested_adjoint_s() {
+    disc_view.d.release();
+    si_view.s.release();
+  }
 };
 
 static SolveParams to_params(const goal_solve_params* p) {
@@ -625,6 +629,7 @@ int goal_nested_adjoint_create(goal_mechanics base, goal_nested_adjoint* out) {
   h->a.build(*base->m);
   h->disc_view.d.reset(h->a.disc.get());
   h->disc_view.owns_stream = false;
+  h->si_view.s.reset(h->a.si.get());
   *out = h.release();
   GOAL_API_END
 }
@@ -633,6 +638,13 @@ int goal_nested_adjoint_disc(goal_nested_adjoint a, goal_disc* nested) {
   GOAL_API_BEGIN
   GOAL_ARG(a && nested, "null argument");
   *nested = &a->disc_view;
+  GOAL_API_END
+}
+
+int goal_nested_adjoint_sol_info(goal_nested_adjoint a, goal_sol_info* s) {
+  GOAL_API_BEGIN
+  GOAL_ARG(a && s, "null argument");
+  *s = &a->si_view;
   GOAL_API_END
 }
 

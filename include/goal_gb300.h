@@ -242,6 +242,8 @@ typedef struct {
 } goal_dwr_result;
 int goal_nested_adjoint_create(goal_mechanics base, goal_nested_adjoint* out);
 int goal_nested_adjoint_disc(goal_nested_adjoint a, goal_disc* nested);
+/* the nested linear objects (dRdu^T after a run), e.g. to attach a learned preconditioner */
+int goal_nested_adjoint_sol_info(goal_nested_adjoint a, goal_sol_info* s);
 int goal_nested_adjoint_run(goal_nested_adjoint a, goal_bcs nested_bcs, int qoi, double rho, double t_now,
                             double t_old, const goal_solve_params* params, goal_dwr_result* result,
                             double* base_error, double* nested_error);

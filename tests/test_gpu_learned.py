@@ -26,22 +26,27 @@ def bsr_host(d, s):
     rp, ci = d.graph()
     N = d.num_nodes
     A = s.dRdu_bsr().reshape(-1, 4, 4)
-    deg = (rp[4:4 * N + 1:4] - rp[0:4 * N:4]) // 4
+    deg = (rp[1:4 * N + 1:4] - rp[0:4 * N:4]) // 4
     brow = np.concatenate([[0], np.cumsum(deg)])
     bcol = np.concatenate([ci[rp[4 * n]:rp[4 * n] + 4 * deg[n]:4] // 4 for n in range(N)])
     diag = np.array([brow[n] + np.searchsorted(bcol[brow[n]:brow[n + 1]], n) for n in range(N)])
     return brow, bcol, diag, A
 
 
-def newton_system(n, load, seed=0):
+def newton_system(n, steps):
+    """The Newton system after ``steps`` J2 load steps (u_x = 0.001 t on x=1)."""
     mesh = kuhn_cube(n)
     d = api.Disc(mesh)
     m = api.Mechanics(d, api.J2, [MAT])
     s = api.SolInfo(d)
-    bcs = api.Bcs(d, [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", f"{load}*t")], [])
-    api.primal_solve(m, s, bcs, 1.0, 0.0, 15, 1e-8, api.solve_params(tolerance=1e-10, precision=api.MIXED))
+    bcs = api.Bcs(d, [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", "0.001*t")], [])
+    for k in range(1, steps + 1):
+        if k > 1:
+            m.update_states()
+        api.primal_solve(m, s, bcs, float(k), float(k - 1), 15, 1e-8,
+                         api.solve_params(tolerance=1e-10, precision=api.MIXED))
     api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, qoi=api.QOI_AVG_DISP)
-    api.set_jac_dbcs(m, s, bcs, 1.0)
+    api.set_jac_dbcs(m, s, bcs, float(steps))
     return d, m, s, bcs
 
 
@@ -72,13 +77,11 @@ def test_forward_and_gradient_match_restatement():
 
 
 def test_training_and_gain_over_block_jacobi():
-    train = [newton_system(8, ld)[2:3][0] for ld in (0.001, 0.002, 0.003)]
-    # keep the systems alive with their discs
-    systems = [newton_system(8, ld) for ld in (0.001, 0.002, 0.003)]
+    systems = [newton_system(8, k) for k in (1, 2, 3)]
     net = api.Learned(seed=0)
     losses = net.train([x[2] for x in systems], epochs=40, lr=2e-3, num_probes=8)
     assert losses[-1] < losses[0]
-    d, m, s, bcs = newton_system(10, 0.0025)  # held out: other mesh, other load
+    d, m, s, bcs = newton_system(10, 2)  # held out: another mesh
     b = s.dMdu
     prm = dict(tolerance=1e-10, max_iters=20000, krylov_size=100)
     x0, plain = api.solve(s, b, params=api.solve_params(**prm))
@@ -91,4 +94,3 @@ def test_training_and_gain_over_block_jacobi():
     # cap: stop the learned run early and finish with plain block-Jacobi
     x2, capped = api.solve(s, b, params=api.solve_params(precond=api.PRECOND_LEARNED, learned_cap=5, **prm))
     assert capped["fell_back"] and capped["converged"]
-    del train
