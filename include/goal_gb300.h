@@ -276,6 +276,26 @@ int goal_learned_train(goal_learned l, const goal_sol_info* systems, int num_sys
 int goal_sol_info_set_learned(goal_sol_info s, goal_learned l);
 int goal_learned_destroy(goal_learned l);
 
+/* ---------------------------------------------------------------- functional without allocation
+ * No counterpart in the reference. The "avg disp" functional
+ * (AvgDisp::at_point, src/goal_avg_disp.cpp:17-21) over a mesh given as the
+ * caller's DEVICE arrays: coords (3 per node), tets (4 node ids per element),
+ * U (4 per node: u_x, u_y, u_z, p). The value is written to the device double
+ * *J on `stream` (a cudaStream_t; NULL = the default stream); the call does not
+ * wait for it. It performs kernel launches only: no device allocation, no
+ * free, no synchronisation. For callers that may not allocate: code running
+ * inside a stream capture, and frameworks that hand all free device memory to
+ * their own pool. The partial sums live in a fixed 128 KiB device array of this
+ * library, which limits a call to 16,777,216 elements (GOAL_ERR_CAPACITY
+ * beyond). The first call on each device, with that device current, looks up
+ * that array's address; make it before any stream capture. Nothing has to be
+ * zeroed beforehand; *J is overwritten. Calls that overlap in time share the
+ * array and race: issue them on one stream or order them with events. A node
+ * id outside [0, num_nodes) makes *J NaN. Same value as goal_assemble with
+ * GOAL_NONE and GOAL_QOI_AVG_DISP up to summation order. */
+int goal_avg_disp_noalloc(const double* coords, const int* tets, const double* U, int num_nodes, int num_elems,
+                          double* J, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
