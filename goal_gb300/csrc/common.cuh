@@ -102,6 +102,13 @@ struct DevBuf {
   }
 };
 
+// grow-only: a buffer is reallocated only when it is smaller than required, so
+// one workspace can serve problems of any size (kernels index with their own n)
+template <typename T>
+inline void need(DevBuf<T>& b, size_t count) {
+  if (b.n < count || !b.ptr) b.alloc(count);
+}
+
 // ---------------------------------------------------------------- device side
 #ifdef __CUDACC__
 // Neumaier-compensated accumulator (sum + running correction).

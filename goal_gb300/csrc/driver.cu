@@ -146,6 +146,7 @@ SolveStats linear_solve(SolInfo& s, const SolveParams& p, const double* b, doubl
     GOAL_REQUIRE(s.learned, GOAL_ERR_STATE, "learned preconditioner requested but no network is attached");
     s.learned->stream = K.stream;
     BsrMatrix M{A, s.A.ptr};
+    block_jacobi_setup(A, s.A.ptr, nullptr, K);
     mpnn_apply_to_block_jacobi(*s.learned, M, K);
     SolveParams q = p;
     if (p.learned_cap > 0) q.max_iters = std::min(p.max_iters, p.learned_cap);

@@ -113,6 +113,26 @@ __global__ void k_bj(int N, const T* __restrict__ Dinv, const T* __restrict__ v,
   }
 }
 
+// Second, weighted block-Jacobi sweep of the learned preconditioner:
+// z += B (v - w) with w = A z, for column j of V and Z (state st; offset 0
+// and no gate without a state).
+template <typename T>
+__global__ void k_second_sweep_col(int N, const T* __restrict__ B, const T* V, long long ldv, const T* __restrict__ w,
+                                   T* Z, long long ldz, const GState* st) {
+  if (st && st->done) return;
+  const long long j = st ? st->j : 0;
+  const T* v = V + j * ldv;
+  T* z = Z + j * ldz;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    int n = i >> 2, r = i & 3;
+    T b0, b1, b2, b3, v0, v1, v2, v3, w0, w1, w2, w3;
+    Vec4<T>::load(B + 16ll * n + 4 * r, b0, b1, b2, b3);
+    Vec4<T>::load(v + 4ll * n, v0, v1, v2, v3);
+    Vec4<T>::load(w + 4ll * n, w0, w1, w2, w3);
+    z[i] += b0 * (v0 - w0) + b1 * (v1 - w1) + b2 * (v2 - w2) + b3 * (v3 - w3);
+  }
+}
+
 // w = A z_j with z_j = column j of Z
 template <typename T>
 __global__ void __launch_bounds__(256) k_spmv_col(int N, const int* __restrict__ brow_ptr,
@@ -453,15 +473,6 @@ Krylov::~Krylov() {
   if (h_scal) cudaFreeHost(h_scal);
 }
 
-namespace {
-// grow-only: a buffer is reallocated only when it is smaller than required, so
-// one workspace can serve solves of any size (kernels index with the solve's n, m)
-template <typename T>
-void need(DevBuf<T>& b, size_t count) {
-  if (b.n < count || !b.ptr) b.alloc(count);
-}
-}  // namespace
-
 void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
   GOAL_REQUIRE(m_ >= 1 && m_ < kMaxM && mi_ >= 1 && mi_ < kMaxM, GOAL_ERR_ARG, "krylov size must be in [1, 255]");
   if (!h_scal) GOAL_CUDA(cudaMallocHost(&h_scal, 64 * sizeof(double)));
@@ -483,6 +494,7 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
     need(V32, nn * (mi_ + 1));
     need(w32, nn);
     need(r32, nn);
+    need(t32, nn);
     need(Hi, (size_t)(mi_ + 1) * mi_);
     need(csi, mi_ + 1);
     need(sni, mi_ + 1);
@@ -500,6 +512,7 @@ int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, K
   need(K.Dinv, 16ull * N);
   need(K.Dinv32, 16ull * N);
   need(K.flag, 8);
+  K.two_sweep = false;
   GOAL_CUDA(cudaMemsetAsync(K.flag.ptr, 0, sizeof(int), K.stream));
   k_bj_setup<<<grid_for(N, 128), 128, 0, K.stream>>>(N, A.diag, vals, dD, K.Dinv.ptr, K.Dinv32.ptr, K.flag.ptr);
   GOAL_CHECK_LAUNCH();
@@ -612,6 +625,13 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       if (!mixed) {
         k_bj_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv.ptr, K.V.ptr, K.Z.ptr, n, st);
         GOAL_CHECK_LAUNCH();
+        if (K.two_sweep) {
+          k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
+          GOAL_CHECK_LAUNCH();
+          k_second_sweep_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc.ptr, K.V.ptr, n, K.w.ptr, K.Z.ptr, n, st);
+          GOAL_CHECK_LAUNCH();
+          out.spmv64++;
+        }
       } else {
         // inner FP32 GMRES on A32 with right block-Jacobi, fixed mi iterations:
         // Z_j = M^-1 V32 y with V32 the inner basis started from V_j
@@ -628,6 +648,15 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
         for (int it = 0; it < mi; ++it) {
           k_bj_colin<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V32.ptr, n, sti, K.r32.ptr);
           GOAL_CHECK_LAUNCH();
+          if (K.two_sweep) {
+            k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
+                                                           K.t32.ptr);
+            GOAL_CHECK_LAUNCH();
+            k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V32.ptr, n, K.t32.ptr,
+                                                                       K.r32.ptr, 0, sti);
+            GOAL_CHECK_LAUNCH();
+            out.spmv32++;
+          }
           // r32 = M^-1 v_it ; w32 = A32 r32 (ld 0 keeps the input at r32)
           k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
                                                          K.w32.ptr);
@@ -640,6 +669,15 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
         GOAL_CHECK_LAUNCH();
         k_bj<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.w32.ptr, K.r32.ptr);
         GOAL_CHECK_LAUNCH();
+        if (K.two_sweep) {
+          k_spmv<float, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, nullptr,
+                                                            K.t32.ptr);
+          GOAL_CHECK_LAUNCH();
+          k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.w32.ptr, 0, K.t32.ptr,
+                                                                     K.r32.ptr, 0, nullptr);
+          GOAL_CHECK_LAUNCH();
+          out.spmv32++;
+        }
         k_f32_to_col<<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.Z.ptr, n, st);
         GOAL_CHECK_LAUNCH();
         out.inner_iters += mi;

@@ -56,9 +56,13 @@ struct Krylov {
   int n = 0, m = 0, mi = 0;
   DevBuf<double> V, Z, w, r, H, cs, sn, g, y, red, scal, dots;
   DevBuf<double> Hi, csi, sni, gi, yi;   // inner (FP32 solve) Hessenberg and rotations
-  DevBuf<float> V32, w32, r32, A32;
+  DevBuf<float> V32, w32, r32, t32, A32;
   DevBuf<double> Dinv;       // 16 x N inverse diagonal blocks (FP64)
   DevBuf<float> Dinv32;
+  // learned two-sweep form: P r = z + B (r - A z), z = D^-1 r (B: 16 x N)
+  bool two_sweep = false;
+  DevBuf<double> Bc;
+  DevBuf<float> Bc32;
   DevBuf<int> flag;
   double* h_scal = nullptr;  // pinned host mirror of a few scalars
   ~Krylov();
@@ -66,7 +70,8 @@ struct Krylov {
 };
 
 // Inverts the 4x4 diagonal blocks of A (optionally plus a correction dD,
-// 16 x N, added before inversion). Returns the number of singular blocks.
+// 16 x N, added before inversion) and selects plain block-Jacobi. Returns the
+// number of singular blocks.
 int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, Krylov& K);
 // FP32 copy of the matrix values for the mixed solve.
 void make_fp32_copy(const BsrView& A, const double* vals, Krylov& K);

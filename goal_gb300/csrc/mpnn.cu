@@ -36,26 +36,44 @@ __global__ void k_to_bf16(int n, const float* p, unsigned short* out) {
   }
 }
 
-// node features, scales and D^-1; x[16] holds log10 s until the mean is removed
+__device__ __forceinline__ double dof_scale(double a) {
+  const double d = fabs(a);
+  return d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+}
+
+// node features, dof scales, Dirichlet row masks and D^-1; x[16] holds
+// log10 max|D_n| until the mean is removed
 __global__ void k_features(int N, const int* brow_ptr, const int* bcol, const int* diag, const double* A, float* x,
-                           double* s, double* Dinv, int* deg) {
+                           double* s, double* sd, double* Dinv, int* deg, int* dmask) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
     const double* D = A + 16ll * diag[n];
+    double sn[4];
+    for (int r = 0; r < 4; ++r) sn[r] = dof_scale(D[5 * r]);
     double smax = 0.0, dn = 0.0;
-    for (int q = 0; q < 16; ++q) { smax = fmax(smax, fabs(D[q])); dn += D[q] * D[q]; }
+    for (int q = 0; q < 16; ++q) {
+      smax = fmax(smax, fabs(D[q]));
+      const double dh = sn[q >> 2] * D[q] * sn[q & 3];
+      x[20ll * n + q] = (float)dh;
+      dn += dh * dh;
+    }
     const double sc = smax > 0.0 ? smax : 1.0;
     s[n] = sc;
-    for (int q = 0; q < 16; ++q) x[20ll * n + q] = (float)(D[q] / sc);
+    for (int r = 0; r < 4; ++r) sd[4ll * n + r] = sn[r];
     double offn = 0.0;
     double offr[4] = {0, 0, 0, 0};
     int nd = 0;
     for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
-      if (bcol[k] == n) continue;
+      const int m = bcol[k];
+      if (m == n) continue;
       ++nd;
+      const double* Dm = A + 16ll * diag[m];
+      double sm[4];
+      for (int c = 0; c < 4; ++c) sm[c] = dof_scale(Dm[5 * c]);
       double f = 0.0;
       for (int q = 0; q < 16; ++q) {
-        double a = A[16ll * k + q];
-        f += a * a;
+        const double a = A[16ll * k + q];
+        const double ah = sn[q >> 2] * a * sm[q & 3];
+        f += ah * ah;
         offr[q >> 2] += fabs(a);
       }
       offn += sqrt(f);
@@ -64,13 +82,14 @@ __global__ void k_features(int N, const int* brow_ptr, const int* bcol, const in
     dn = sqrt(dn);
     x[20ll * n + 16] = (float)log10(sc);
     x[20ll * n + 17] = (float)(offn / (dn > 0.0 ? dn : 1.0));
-    float flag = 0.0f;
+    int mask = 0;
     for (int r = 0; r < 4; ++r) {
       bool unit = true;
       for (int c = 0; c < 4; ++c) unit = unit && (D[4 * r + c] == (r == c ? 1.0 : 0.0));
-      if (unit && offr[r] == 0.0) flag = 1.0f;
+      if (unit && offr[r] == 0.0) mask |= 1 << r;
     }
-    x[20ll * n + 18] = flag;
+    dmask[n] = mask;
+    x[20ll * n + 18] = (float)(__popc(mask) * 0.25);
     x[20ll * n + 19] = (float)((brow_ptr[n + 1] - brow_ptr[n] - 1) / 16.0);
     // D^-1 (Gauss-Jordan with partial pivoting; identity for a singular block)
     double a[4][8];
@@ -171,28 +190,27 @@ __device__ void load_layer(LayerSmem& sm, const unsigned short* wl) {
   __syncthreads();
 }
 
-// stage [e_nm; h_m] of edge k in sm.in[w]
-__device__ __forceinline__ void stage_edge(LayerSmem& sm, int w, int lane, const double* A, long long k, double sn,
-                                           double smm, const float* h, int m) {
-  if (lane < kME) sm.in[w][lane] = (float)(A[16ll * k + lane] / sqrt(sn * smm));
+// stage [e_nm; h_m] of edge k = (n, m) in sm.in[w]; e_nm = S_n A_nm S_m
+__device__ __forceinline__ void stage_edge(LayerSmem& sm, int w, int lane, const double* A, long long k,
+                                           const double* sd, int n, const float* h, int m) {
+  if (lane < kME) sm.in[w][lane] = (float)(sd[4ll * n + (lane >> 2)] * A[16ll * k + lane] * sd[4ll * m + (lane & 3)]);
   sm.in[w][kME + lane] = h[32ll * m + lane];
   __syncwarp();
 }
 
 __global__ void __launch_bounds__(256) k_layer_fwd(int N, const int* brow_ptr, const int* bcol, const double* A,
-                                                    const double* s, const int* deg, const unsigned short* wl,
+                                                    const double* sd, const int* deg, const unsigned short* wl,
                                                     const float* h_in, float* h_out, float* tbuf, float* ubuf,
                                                     float* aggbuf) {
   __shared__ LayerSmem sm;
   load_layer(sm, wl);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += (gridDim.x * blockDim.x) >> 5) {
-    const double sn = s[n];
     float agg = 0.0f;
     for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
       const int m = bcol[k];
       if (m == n) continue;
-      stage_edge(sm, w, lane, A, k, sn, s[m], h_in, m);
+      stage_edge(sm, w, lane, A, k, sd, n, h_in, m);
       float t = sm.be[lane];
       for (int q = 0; q < kME + kMH; ++q) t += sm.We[lane][q] * sm.in[w][q];
       if (tbuf) tbuf[32ll * k + lane] = t;
@@ -265,26 +283,52 @@ __global__ void k_bsr_mv_t(int N, const int* brow_ptr, const int* bcol, const in
     y[i] = acc;
   }
 }
-// y_n = (D^-1_n + C_n / s_n) v_n
-__global__ void k_apply_P(int N, const double* Dinv, const float* C, const double* s, const double* v, double* y) {
+// y = D^-1 x
+__global__ void k_bjn(int N, const double* Dinv, const double* x, double* y) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
     int n = i >> 2, r = i & 3;
     double acc = 0.0;
-    for (int c = 0; c < 4; ++c) {
-      double p = Dinv[16ll * n + 4 * r + c] + (C ? (double)C[16ll * n + 4 * r + c] / s[n] : 0.0);
-      acc += p * v[4ll * n + c];
-    }
+    for (int c = 0; c < 4; ++c) acc += Dinv[16ll * n + 4 * r + c] * x[4ll * n + c];
     y[i] = acc;
   }
 }
-__global__ void k_axpy(long long n, double a, const double* x, double* y) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    y[i] += a * x[i];
+__device__ __forceinline__ bool kept(const int* dmask, int n, int r) { return ((dmask[n] >> r) & 1) == 0; }
+// probe w (scaled residual space) -> residual-space q = S^-1 w on the non-Dirichlet rows
+__global__ void k_probe(int N, const double* sd, const int* dmask, double* v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x)
+    v[i] = kept(dmask, i >> 2, i & 3) ? v[i] / sd[i] : 0.0;
 }
-__global__ void k_dot_part2(long long n, const double* a, const double* b, double* part) {
-  KSum acc;
+// chat = (D^-1 t) / S ; y = z + S W chat   (W = C with Dirichlet rows/columns zeroed)
+__global__ void k_second_sweep(int N, const double* Dinv, const double* sd, const int* dmask, const float* C,
+                               const double* t, const double* z, double* chat, double* y) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    double ch[4];
+    for (int r = 0; r < 4; ++r) {
+      double acc = 0.0;
+      for (int c = 0; c < 4; ++c) acc += Dinv[16ll * n + 4 * r + c] * t[4ll * n + c];
+      ch[r] = acc / sd[4ll * n + r];
+      chat[4ll * n + r] = ch[r];
+    }
+    for (int r = 0; r < 4; ++r) {
+      double acc = 0.0;
+      if (kept(dmask, n, r))
+        for (int c = 0; c < 4; ++c)
+          if (kept(dmask, n, c)) acc += (double)C[16ll * n + 4 * r + c] * ch[c];
+      y[4ll * n + r] = z[4ll * n + r] + sd[4ll * n + r] * acc;
+    }
+  }
+}
+__global__ void k_scale_by(long long n, const double* sd, double* x) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    acc.add(a[i] * b[i]);
+    x[i] *= sd[i];
+}
+// sum of (w_i a_i)^2
+__global__ void k_wnorm_part(long long n, const double* a, const double* w, double* part) {
+  KSum acc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double t = w[i] * a[i];
+    acc.add(t * t);
+  }
   acc = block_reduce(acc);
   if (threadIdx.x == 0) { part[2 * blockIdx.x] = acc.s; part[2 * blockIdx.x + 1] = acc.c; }
 }
@@ -299,17 +343,17 @@ __global__ void k_fin2(const double* part, int nb, double* out) {
   acc = block_reduce(acc);
   if (threadIdx.x == 0) out[0] = acc.value();
 }
-// dP_n += coef g_n v_n^T with coef = -2 / |v|^2 ; loss += |r|^2 / |v|^2
-__global__ void k_dP(int N, const double* g, const double* v, const double* vv, double* dP) {
-  const double coef = -2.0 / vv[0];
+// dW_n += (-2 / |S v|^2) (S g)_n chat_n^T on the kept rows/columns; g = A^T (S e)
+__global__ void k_dW(int N, const double* g, const double* sd, const double* chat, const int* dmask,
+                     const double* nv, double* dW) {
+  const double coef = -2.0 / nv[0];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) {
     int n = i >> 4, r = (i >> 2) & 3, c = i & 3;
-    dP[i] += coef * g[4ll * n + r] * v[4ll * n + c];
+    if (kept(dmask, n, r) && kept(dmask, n, c)) dW[i] += coef * sd[4ll * n + r] * g[4ll * n + r] * chat[4ll * n + c];
   }
 }
-__global__ void k_dC(int N, const double* dP, const double* s, float* dC) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x)
-    dC[i] = (float)(dP[i] / s[i >> 4]);
+__global__ void k_dC(int N, const double* dW, float* dC) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) dC[i] = (float)dW[i];
 }
 
 // ---------------------------------------------------------------- backward
@@ -377,7 +421,7 @@ __global__ void __launch_bounds__(256) k_layer_bwd_node(int N, const unsigned sh
 
 // edge part: dt, dWe, dbe and g_k = (We^T dt)[16:] for every edge k = (n, m)
 __global__ void __launch_bounds__(256) k_layer_bwd_edge(int N, const int* brow_ptr, const int* bcol, const double* A,
-                                                         const double* s, const unsigned short* wl, int woff,
+                                                         const double* sd, const unsigned short* wl, int woff,
                                                          const float* h_in, const float* tbuf, const float* dagg,
                                                          float* gbuf, float* part, int P) {
   __shared__ LayerSmem sm;
@@ -388,12 +432,11 @@ __global__ void __launch_bounds__(256) k_layer_bwd_edge(int N, const int* brow_p
   for (int q = 0; q < kME + kMH; ++q) gW[q] = 0.0f;
   float gb = 0.0f;
   for (int n = gw; n < N; n += (gridDim.x * blockDim.x) >> 5) {
-    const double sn = s[n];
     const float da = dagg[32ll * n + lane];
     for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
       const int m = bcol[k];
       if (m == n) continue;
-      stage_edge(sm, w, lane, A, k, sn, s[m], h_in, m);
+      stage_edge(sm, w, lane, A, k, sd, n, h_in, m);
       const float dt = (tbuf[32ll * k + lane] > 0.0f) ? da : 0.0f;
       sm.d[w][lane] = dt;
       __syncwarp();
@@ -463,9 +506,17 @@ __global__ void k_adam(int n, float* p, const float* g, float* m1, float* m2, fl
   }
 }
 
-__global__ void k_write_bj(int N, const double* Dinv, const float* C, const double* s, double* out64, float* out32) {
+// B_n = S_n W_n S_n^-1 D_n^-1 (W = C with Dirichlet rows/columns zeroed)
+__global__ void k_write_B(int N, const double* Dinv, const float* C, const double* sd, const int* dmask,
+                          double* out64, float* out32) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) {
-    double v = Dinv[i] + (double)C[i] / s[i >> 4];
+    int n = i >> 4, r = (i >> 2) & 3, c = i & 3;
+    double acc = 0.0;
+    if (kept(dmask, n, r))
+      for (int k = 0; k < 4; ++k)
+        if (kept(dmask, n, k))
+          acc += (double)C[16ll * n + 4 * r + k] / sd[4ll * n + k] * Dinv[16ll * n + 4 * k + c];
+    const double v = sd[4ll * n + r] * acc;
     out64[i] = v;
     out32[i] = (float)v;
   }
@@ -521,13 +572,17 @@ void Mpnn::reserve(int N, int nnzb) {
     dh.alloc(32ll * N);
     dagg.alloc(32ll * N);
     s.alloc(N);
+    sd.alloc(4ll * N);
     Dinv.alloc(16ll * N);
     dP.alloc(16ll * N);
     y.alloc(4ll * N);
     r.alloc(4ll * N);
     gT.alloc(4ll * N);
     v.alloc(4ll * N);
+    z.alloc(4ll * N);
+    chat.alloc(4ll * N);
     deg.alloc(N);
+    dmask.alloc(N);
     cap_nodes = N;
   }
   if (nnzb > cap_blocks) {
@@ -546,7 +601,7 @@ void mpnn_forward(Mpnn& net, const BsrMatrix& A, bool keep) {
   cudaStream_t st = net.stream;
   net.reserve(N, A.v.nnzb);
   k_features<<<grid_for(N, 128), 128, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.v.diag, A.vals, net.x.ptr, net.s.ptr,
-                                               net.Dinv.ptr, net.deg.ptr);
+                                               net.sd.ptr, net.Dinv.ptr, net.deg.ptr, net.dmask.ptr);
   GOAL_CHECK_LAUNCH();
   const int nb = std::min(grid_for(N, 256), 1024);
   k_sum_log<<<nb, 256, 0, st>>>(N, net.x.ptr, net.red.ptr);
@@ -561,7 +616,7 @@ void mpnn_forward(Mpnn& net, const BsrMatrix& A, bool keep) {
     const unsigned short* wl = net.wbf.ptr + MpnnLayout::L0 + l * MpnnLayout::layer;
     float* hin = hbase + 32ll * N * l;
     float* hout = hbase + 32ll * N * (l + 1);
-    k_layer_fwd<<<wgrid, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.s.ptr, net.deg.ptr, wl, hin, hout,
+    k_layer_fwd<<<wgrid, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.sd.ptr, net.deg.ptr, wl, hin, hout,
                                        keep ? net.t.ptr + 32ll * A.v.nnzb * l : nullptr,
                                        keep ? net.u.ptr + 32ll * N * l : nullptr,
                                        keep ? net.agg.ptr + 32ll * N * l : nullptr);
@@ -581,7 +636,9 @@ double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const doubl
   net.dP.zero(st);
   const int vg = grid_for(n, 256);
   const int nb = std::min(grid_for(n, 256), 1024);
-  double* scal = net.red.ptr + 2 * 1024 + 2;  // [vv, rr]
+  double* scal = net.red.ptr + 2 * 1024 + 2;  // [|S v|^2, |S e|^2]
+  const int* bp = A.v.brow_ptr;
+  const int* bc = A.v.bcol;
   double loss = 0.0;
   for (int p = 0; p < num_probes; ++p) {
     if (probes_dev) {
@@ -589,39 +646,49 @@ double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const doubl
     } else {
       k_gauss<<<vg, 256, 0, st>>>(n, seed + 7919u * (unsigned)p, net.v.ptr);
       GOAL_CHECK_LAUNCH();
-      if (p & 1) {  // smoothed probe: three damped block-Jacobi sweeps
-        for (int it = 0; it < 3; ++it) {
-          k_bsr_mv<<<vg, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.v.ptr, net.r.ptr, nullptr);
-          GOAL_CHECK_LAUNCH();
-          k_apply_P<<<vg, 256, 0, st>>>(N, net.Dinv.ptr, nullptr, net.s.ptr, net.r.ptr, net.y.ptr);
-          GOAL_CHECK_LAUNCH();
-          k_axpy<<<vg, 256, 0, st>>>(n, -0.6, net.y.ptr, net.v.ptr);
-          GOAL_CHECK_LAUNCH();
-        }
-      }
     }
-    k_apply_P<<<vg, 256, 0, st>>>(N, net.Dinv.ptr, net.C.ptr, net.s.ptr, net.v.ptr, net.y.ptr);
+    k_probe<<<vg, 256, 0, st>>>(N, net.sd.ptr, net.dmask.ptr, net.v.ptr);
     GOAL_CHECK_LAUNCH();
-    k_bsr_mv<<<vg, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.y.ptr, net.r.ptr, net.v.ptr);
+    if (p & 1) {  // v = A D^-1 q
+      k_bjn<<<vg, 256, 0, st>>>(N, net.Dinv.ptr, net.v.ptr, net.z.ptr);
+      GOAL_CHECK_LAUNCH();
+      k_bsr_mv<<<vg, 256, 0, st>>>(N, bp, bc, A.vals, net.z.ptr, net.v.ptr, nullptr);
+      GOAL_CHECK_LAUNCH();
+    }
+    // z = D^-1 v ; r = v - A z ; y = z + S W chat with chat = D^-1 r / S
+    k_bjn<<<vg, 256, 0, st>>>(N, net.Dinv.ptr, net.v.ptr, net.z.ptr);
     GOAL_CHECK_LAUNCH();
-    k_bsr_mv_t<<<vg, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, net.tmap.ptr, A.vals, net.r.ptr, net.gT.ptr);
+    k_bsr_mv<<<vg, 256, 0, st>>>(N, bp, bc, A.vals, net.z.ptr, net.r.ptr, net.v.ptr);
     GOAL_CHECK_LAUNCH();
-    k_dot_part2<<<nb, 256, 0, st>>>(n, net.v.ptr, net.v.ptr, net.red.ptr);
+    k_second_sweep<<<grid_for(N, 128), 128, 0, st>>>(N, net.Dinv.ptr, net.sd.ptr, net.dmask.ptr, net.C.ptr, net.r.ptr,
+                                                     net.z.ptr, net.chat.ptr, net.y.ptr);
+    GOAL_CHECK_LAUNCH();
+    // e = S (v - A y) ; g = A^T (S e)
+    k_bsr_mv<<<vg, 256, 0, st>>>(N, bp, bc, A.vals, net.y.ptr, net.r.ptr, net.v.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_wnorm_part<<<nb, 256, 0, st>>>(n, net.v.ptr, net.sd.ptr, net.red.ptr);
     GOAL_CHECK_LAUNCH();
     k_fin2<<<1, 1024, 0, st>>>(net.red.ptr, nb, scal);
     GOAL_CHECK_LAUNCH();
-    k_dot_part2<<<nb, 256, 0, st>>>(n, net.r.ptr, net.r.ptr, net.red.ptr);
+    k_wnorm_part<<<nb, 256, 0, st>>>(n, net.r.ptr, net.sd.ptr, net.red.ptr);
     GOAL_CHECK_LAUNCH();
     k_fin2<<<1, 1024, 0, st>>>(net.red.ptr, nb, scal + 1);
     GOAL_CHECK_LAUNCH();
-    k_dP<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.gT.ptr, net.v.ptr, scal, net.dP.ptr);
+    k_scale_by<<<vg, 256, 0, st>>>(n, net.sd.ptr, net.r.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_scale_by<<<vg, 256, 0, st>>>(n, net.sd.ptr, net.r.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_bsr_mv_t<<<vg, 256, 0, st>>>(N, bp, bc, net.tmap.ptr, A.vals, net.r.ptr, net.gT.ptr);
+    GOAL_CHECK_LAUNCH();
+    k_dW<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.gT.ptr, net.sd.ptr, net.chat.ptr, net.dmask.ptr, scal,
+                                                  net.dP.ptr);
     GOAL_CHECK_LAUNCH();
     double hv[2];
     GOAL_CUDA(cudaMemcpyAsync(hv, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     GOAL_CUDA(cudaStreamSynchronize(st));
     loss += hv[1] / hv[0];
   }
-  k_dC<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.dP.ptr, net.s.ptr, net.dC.ptr);
+  k_dC<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.dP.ptr, net.dC.ptr);
   GOAL_CHECK_LAUNCH();
   // backward
   const int P = MpnnLayout::total;
@@ -640,7 +707,7 @@ double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const doubl
                                                    net.agg.ptr + 32ll * N * l, net.deg.ptr, net.dh.ptr, dh_acc.ptr,
                                                    net.dagg.ptr, net.part.ptr, P);
     GOAL_CHECK_LAUNCH();
-    k_layer_bwd_edge<<<kGridBlocks, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.s.ptr, wl, woff, hin,
+    k_layer_bwd_edge<<<kGridBlocks, 256, 0, st>>>(N, A.v.brow_ptr, A.v.bcol, A.vals, net.sd.ptr, wl, woff, hin,
                                                    net.t.ptr + 32ll * A.v.nnzb * l, net.dagg.ptr, net.gbuf.ptr,
                                                    net.part.ptr, P);
     GOAL_CHECK_LAUNCH();
@@ -669,11 +736,12 @@ void mpnn_adam(Mpnn& net, float lr, float beta1, float beta2, float eps) {
 void mpnn_apply_to_block_jacobi(Mpnn& net, const BsrMatrix& A, Krylov& K) {
   const int N = A.v.num_nodes;
   mpnn_forward(net, A, false);
-  if (K.Dinv.n < 16ull * N) K.Dinv.alloc(16ll * N);
-  if (K.Dinv32.n < 16ull * N) K.Dinv32.alloc(16ll * N);
-  k_write_bj<<<grid_for(16ll * N, 256), 256, 0, net.stream>>>(N, net.Dinv.ptr, net.C.ptr, net.s.ptr, K.Dinv.ptr,
-                                                              K.Dinv32.ptr);
+  need(K.Bc, 16ull * N);
+  need(K.Bc32, 16ull * N);
+  k_write_B<<<grid_for(16ll * N, 256), 256, 0, net.stream>>>(N, net.Dinv.ptr, net.C.ptr, net.sd.ptr, net.dmask.ptr,
+                                                             K.Bc.ptr, K.Bc32.ptr);
   GOAL_CHECK_LAUNCH();
+  K.two_sweep = true;
 }
 
 }  // namespace goal

@@ -4,16 +4,20 @@
 // It has no counterpart in the reference (goal preconditions with MueLu AMG,
 // src/goal_linear_solve.cpp:59-65).
 //
-//   s_n   = max |D_n|,  x_n = [D_n/s_n, log10 s_n - mean, offdiag/diag norm ratio,
-//                              Dirichlet flag, (deg-1)/16]               (20 features)
-//   e_nm  = A_nm / sqrt(s_n s_m)                                           (16 features)
+// The network sees the dof-scaled matrix A^ = S A S, S = diag(|a_ii|^-1/2),
+// in which displacement and pressure rows are comparable:
+//   x_n   = [D^_n, log10 max|D_n| - mean, offdiag/diag norm ratio of A^,
+//            fraction of Dirichlet rows, (deg-1)/16]                (20 features)
+//   e_nm  = A^_nm                                                   (16 features)
 //   h0    = relu(W0 x + b0)
 //   x3 layers: t_nm = We [e_nm; h_m] + be,  agg_n = mean_m relu(t_nm),
 //              h_n += relu(Wu [h_n; agg_n] + bu)
-//   C_n   = Wd h_n + bd;   preconditioner block P_n = D_n^-1 + C_n / s_n
-// Training loss for probe vectors v: sum_v |v - A P v|^2 / |v|^2 (P acts as a
-// right preconditioner). Wd, bd start at zero, so the untrained network is
-// plain block-Jacobi.
+//   W_n   = Wd h_n + bd, rows/columns of Dirichlet (identity) rows zeroed
+// and weights the second of two block-Jacobi sweeps node by node:
+//   z = D^-1 r,   P r = z + B (r - A z),   B_n = S_n W_n S_n^-1 D_n^-1.
+// Training loss for probes w_i (scaled residual space): v_i = S^-1 w_i (even
+// i) or A D^-1 S^-1 w_i (odd i), L = sum_i |S(v_i - A P v_i)|^2 / |S v_i|^2.
+// Wd, bd start at zero, so the untrained network is plain block-Jacobi.
 #pragma once
 
 #include "common.cuh"
@@ -48,8 +52,8 @@ struct Mpnn {
   long long adam_t = 0;
   // per-graph work buffers
   DevBuf<float> x, h, t, u, agg, C, dC, dh, dagg, gbuf, grad, part;
-  DevBuf<double> s, Dinv, dP, y, r, gT, v, red;
-  DevBuf<int> tmap, deg;
+  DevBuf<double> s, sd, Dinv, dP, y, r, gT, v, z, chat, red;
+  DevBuf<int> tmap, deg, dmask;
   int cap_nodes = 0, cap_blocks = 0;
   void init(int seed);
   void upload();                        // host_params -> device (+ bfloat16 copy)
@@ -62,15 +66,18 @@ struct BsrMatrix {
   const double* vals;
 };
 
-// Corrections C (16 x N floats, node-major) of the network for matrix A; also
-// leaves the node scales s and D^-1 in the network's buffers.
+// Network outputs C (16 x N floats, node-major: W_n before masking) for matrix
+// A; also leaves the dof scales S, D^-1 and the Dirichlet row masks in the
+// network's buffers.
 void mpnn_forward(Mpnn& net, const BsrMatrix& A, bool keep);
 // Loss and parameter gradient (into net.grad) for the probe vectors (host or
 // generated from seed when probes == nullptr).
 double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const double* probes_dev, unsigned seed);
 // Adam step on net.params with net.grad.
 void mpnn_adam(Mpnn& net, float lr, float beta1, float beta2, float eps);
-// Writes D^-1 + C/s into Krylov's block-Jacobi buffers (FP64 and FP32).
+// Writes the second-sweep blocks B (FP64 and FP32) into the Krylov workspace
+// and switches its preconditioner to the two-sweep form; the plain D^-1
+// blocks must already be set up (block_jacobi_setup).
 void mpnn_apply_to_block_jacobi(Mpnn& net, const BsrMatrix& A, Krylov& K);
 
 }  // namespace goal

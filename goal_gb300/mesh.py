@@ -87,8 +87,13 @@ def _plane_sets(coords: np.ndarray, tets: np.ndarray, lo: np.ndarray, hi: np.nda
     return node_sets, side_sets
 
 
-def kuhn_cube(n: int, length=(1.0, 1.0, 1.0), set_name: str = "cube") -> Mesh:
-    """Structured n x n x n hex grid of [0,Lx]x[0,Ly]x[0,Lz], 6 Kuhn tets per hex."""
+def kuhn_cube(n: int, length=(1.0, 1.0, 1.0), set_name: str = "cube", jitter: float = 0.0, seed: int = 0) -> Mesh:
+    """Structured n x n x n hex grid of [0,Lx]x[0,Ly]x[0,Lz], 6 Kuhn tets per hex.
+
+    jitter > 0 moves every interior node by a seeded uniform offset in
+    [-jitter, jitter] x (grid spacing) per coordinate, which removes the
+    translation symmetry of the grid (boundary nodes stay on their faces);
+    jitter <= 0.25 keeps every tet positively oriented."""
     n1 = n + 1
     g = np.arange(n1, dtype=np.float64) / n
     X, Y, Z = np.meshgrid(g * length[0], g * length[1], g * length[2], indexing="ij")
@@ -110,6 +115,14 @@ def kuhn_cube(n: int, length=(1.0, 1.0, 1.0), set_name: str = "cube") -> Mesh:
     tets = np.stack(tets, axis=1).reshape(-1, 4).astype(np.int32)
     tets = orient_positive(coords, tets)
     node_sets, side_sets = _plane_sets(coords, tets, np.zeros(3), np.array(length, float), 1e-12)
+    if jitter > 0.0:
+        if jitter > 0.25:
+            raise ValueError("jitter above 0.25 can invert tets")
+        L = np.array(length, float)
+        interior = np.all((coords > 1e-12 * L) & (coords < L - 1e-12 * L), axis=1)
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter, jitter, size=coords.shape) * (L / n)
+        coords = coords + d * interior[:, None]
     return Mesh(coords=np.ascontiguousarray(coords), tets=tets,
                 elem_set=np.zeros(tets.shape[0], np.int32), elem_set_names=[set_name],
                 node_sets=node_sets, side_sets=side_sets)

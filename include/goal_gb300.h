@@ -253,22 +253,26 @@ int goal_nested_adjoint_destroy(goal_nested_adjoint a);
 
 /* ---------------------------------------------------------------- learned preconditioner
  * A mesh-graph network (3 message-passing layers, width 32, bfloat16 weights,
- * float32 arithmetic) that emits a correction C_n for every node's block of the
- * block-Jacobi preconditioner: P_n = D_n^-1 + C_n / max|D_n|. It has no
- * counterpart in the reference (goal preconditions with MueLu AMG,
- * src/goal_linear_solve.cpp:59-65). Training minimizes sum_v |v - A P v|^2/|v|^2
- * over probe vectors on the GPU with Adam. A solve with precond = 1 uses the
- * network attached to the SolInfo. */
+ * float32 arithmetic) on the matrix's node graph, in the dof-scaled space
+ * S A S (S = diag(|a_ii|^-1/2)). It emits a 4x4 block W_n per node that
+ * weights a second block-Jacobi sweep: z = D^-1 r, P r = z + B (r - A z),
+ * B_n = S_n W_n S_n^-1 D_n^-1 (rows/columns of Dirichlet rows zeroed). It has
+ * no counterpart in the reference (goal preconditions with MueLu AMG,
+ * src/goal_linear_solve.cpp:59-65). Training minimizes
+ * sum_i |S(v_i - A P v_i)|^2 / |S v_i|^2 over probes (v_i = S^-1 w_i or
+ * A D^-1 S^-1 w_i) on the GPU with Adam; the untrained network (decoder at
+ * zero) is plain block-Jacobi. A solve with precond = 1 uses the network
+ * attached to the SolInfo. */
 typedef struct goal_learned_s* goal_learned;
 int goal_learned_create(int seed, goal_learned* out);
 int goal_learned_num_params(goal_learned l, int* n);
 int goal_learned_get_params(goal_learned l, float* params);
 int goal_learned_set_params(goal_learned l, const float* params);
 /* loss and gradient for the SolInfo's matrix; probes: num_probes x num_dofs host
- * values, or NULL to draw them from seed (half of them smoothed) */
+ * values w_i (scaled residual space), or NULL to draw them from seed */
 int goal_learned_loss_grad(goal_learned l, goal_sol_info s, int num_probes, const double* probes, int seed,
                            double* loss, float* grad);
-/* corrections C (16 per node, row-major 4x4) for the SolInfo's matrix */
+/* network outputs W (16 per node, row-major 4x4, before the Dirichlet masking) for the SolInfo's matrix */
 int goal_learned_corrections(goal_learned l, goal_sol_info s, float* C);
 /* epochs x (one Adam step per system); losses[epochs] = summed loss per epoch */
 int goal_learned_train(goal_learned l, const goal_sol_info* systems, int num_systems, int epochs, float lr,

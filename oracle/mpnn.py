@@ -6,16 +6,25 @@ statement of the CUDA forward/backward kernels, used to check their outputs
 and gradients.
 
 Graph: nodes of the mesh, edges = off-diagonal 4x4 blocks of the matrix.
-  s_n      = max |D_n|                      (D_n diagonal block)
-  x_n      = [D_n / s_n (16), log10 s_n - mean, offdiag row ratio, dirichlet flag, deg/16]   (20)
-  e_nm     = A_nm / sqrt(s_n s_m)           (16)
+Everything the network sees is in the dof-scaled space A^ = S A S with
+S = diag(|a_ii|^-1/2), where displacement and pressure rows are comparable.
+  x_n      = [D^_n (16), log10 max|D_n| - mean, offdiag/diag ratio of A^,
+              fraction of Dirichlet rows, (deg-1)/16]                  (20)
+  e_nm     = A^_nm                                                     (16)
   h0       = relu(W0 x + b0)                                          (32)
   layer l  : t_nm = We_l [e_nm; h_m] + be_l ; agg_n = mean_m relu(t_nm)
              h_n <- h_n + relu(Wu_l [h_n; agg_n] + bu_l)                (3 layers)
-  C_n      = Wd h_n + bd                                              (16)
-  P_n      = D_n^-1 + C_n / s_n          (block of the preconditioner, z_n = P_n r_n)
+  C_n      = Wd h_n + bd      = W_n, a 4x4 block in the scaled space, with
+             the rows and columns of Dirichlet (identity) rows zeroed  (16)
+Preconditioner: two block-Jacobi sweeps, the second one weighted per node,
+  z = D^-1 r,   P r = z + S W S^-1 D^-1 (r - A z)
+i.e. P = D^-1 + B (I - A D^-1) with B_n = S_n W_n S_n^-1 D_n^-1. W = 0 (the
+untrained network: the decoder starts at zero) is plain block-Jacobi.
+Loss for probes w_i (scaled residual space, Dirichlet rows zeroed): with
+v_i = S^-1 w_i for even i and v_i = A D^-1 S^-1 w_i for odd i (weighted toward
+the high end of the spectrum, the part a node-local preconditioner acts on),
+  L = sum_i |S (v_i - A P v_i)|^2 / |S v_i|^2.
 Weights are used rounded to bfloat16 (round to nearest even); all sums in float32.
-Loss for probes v:  L = sum_v |v - A P v|^2 / |v|^2.
 """
 from __future__ import annotations
 
@@ -64,33 +73,36 @@ def bf16(a):
 
 
 def features(brow_ptr, bcol, diag, A):
-    """A: (nnzb, 4, 4) float64 blocks. Returns x (N,20) f32, e (nnzb,16) f32, s (N) f64, Dinv (N,4,4)."""
+    """A: (nnzb, 4, 4) float64 blocks. Returns x (N,20) f32, e (nnzb,16) f32,
+    sd (N,4) f64 = |a_ii|^-1/2, Dinv (N,4,4), dirichlet (N,4) bool."""
     N = len(brow_ptr) - 1
     D = A[diag]
-    s = np.abs(D).reshape(N, 16).max(axis=1)
-    s = np.where(s > 0, s, 1.0)
+    dd = np.abs(np.einsum("nii->ni", D))
+    sd = np.where(dd > 0, 1.0 / np.sqrt(np.where(dd > 0, dd, 1.0)), 1.0)
     rows = np.repeat(np.arange(N), np.diff(brow_ptr))
     off = bcol != rows
+    Ah = A * sd[rows][:, :, None] * sd[bcol][:, None, :]
+    Dh = Ah[diag]
+    s = np.abs(D).reshape(N, 16).max(axis=1)
+    s = np.where(s > 0, s, 1.0)
     offn = np.zeros(N)
-    np.add.at(offn, rows[off], np.sqrt((A[off] ** 2).sum(axis=(1, 2))))
-    dn = np.sqrt((D ** 2).sum(axis=(1, 2)))
+    np.add.at(offn, rows[off], np.sqrt((Ah[off] ** 2).sum(axis=(1, 2))))
+    dn = np.sqrt((Dh ** 2).sum(axis=(1, 2)))
+    # Dirichlet row: a unit row of the diagonal block with no off-diagonal entries
+    offr = np.zeros((N, 4))
+    np.add.at(offr, rows[off], np.abs(A[off]).sum(axis=2))
+    unit = np.abs(D - np.eye(4)[None]).max(axis=2) == 0
+    dirichlet = unit & (offr == 0)
     ls = np.log10(s)
     x = np.zeros((N, NF))
-    x[:, :16] = (D / s[:, None, None]).reshape(N, 16)
+    x[:, :16] = Dh.reshape(N, 16)
     x[:, 16] = ls - ls.mean()
     x[:, 17] = offn / np.where(dn > 0, dn, 1.0)
-    # Dirichlet row: a row of the node that is a unit vector with no off-diagonal entries
-    dir_flag = np.zeros(N)
-    for r in range(4):
-        unit = (np.abs(D[:, r, :] - np.eye(4)[r]).max(axis=1) == 0)
-        offr = np.zeros(N)
-        np.add.at(offr, rows[off], np.abs(A[off][:, r, :]).sum(axis=1))
-        dir_flag = np.maximum(dir_flag, (unit & (offr == 0)).astype(float))
-    x[:, 18] = dir_flag
+    x[:, 18] = dirichlet.sum(axis=1) / 4.0
     x[:, 19] = (np.diff(brow_ptr) - 1) / 16.0
-    e = (A / np.sqrt(s[rows] * s[bcol])[:, None, None]).reshape(-1, 16)
+    e = Ah.reshape(-1, 16)
     Dinv = np.linalg.inv(D)
-    return x.astype(np.float32), e.astype(np.float32), s, Dinv
+    return x.astype(np.float32), e.astype(np.float32), sd, Dinv, dirichlet
 
 
 def forward(params, brow_ptr, bcol, diag, x, e, keep=False):
@@ -122,8 +134,21 @@ def forward(params, brow_ptr, bcol, diag, x, e, keep=False):
     return C.astype(np.float32)
 
 
-def blocks(C, s, Dinv):
-    return Dinv + C.reshape(-1, 4, 4).astype(np.float64) / s[:, None, None]
+def masked(C, dirichlet):
+    keep = (~dirichlet).astype(np.float64)
+    return C.reshape(-1, 4, 4).astype(np.float64) * keep[:, :, None] * keep[:, None, :]
+
+
+def blocks(C, sd, Dinv, dirichlet):
+    """B_n = S_n W_n S_n^-1 D_n^-1 (the weighted second sweep)."""
+    W = masked(C, dirichlet)
+    return np.einsum("nik,nkj->nij", sd[:, :, None] * W / sd[:, None, :], Dinv)
+
+
+def apply_P(brow_ptr, bcol, A, Dinv, B, r):
+    z = np.einsum("nij,nj->ni", Dinv, r.reshape(-1, 4)).ravel()
+    u = r - apply_bsr(brow_ptr, bcol, A, z)
+    return z + np.einsum("nij,nj->ni", B, u.reshape(-1, 4)).ravel()
 
 
 def apply_bsr(brow_ptr, bcol, A, y):
@@ -143,23 +168,29 @@ def apply_bsr_t(brow_ptr, bcol, A, y):
 
 
 def loss_and_grad(flat, brow_ptr, bcol, diag, A, probes):
-    """Loss sum_v |v - A P v|^2/|v|^2 and its gradient w.r.t. the (float32) parameters."""
+    """Loss sum_w |S(v - A P v)|^2/|S v|^2 (v = A D^-1 S^-1 w) and its gradient
+    w.r.t. the (float32) parameters."""
     params = unflatten(np.asarray(flat, np.float32))
-    x, e, s, Dinv = features(brow_ptr, bcol, diag, A)
+    x, e, sd, Dinv, dirichlet = features(brow_ptr, bcol, diag, A)
     C, cache = forward(params, brow_ptr, bcol, diag, x, e, keep=True)
-    P = blocks(C, s, Dinv)
+    W = masked(C, dirichlet)
     N = len(brow_ptr) - 1
+    keep = (~dirichlet).astype(np.float64)
     L = 0.0
-    dP = np.zeros((N, 4, 4))
-    for v in probes:
-        vn = v.reshape(-1, 4)
-        y = np.einsum("nij,nj->ni", P, vn).ravel()
-        r = v - apply_bsr(brow_ptr, bcol, A, y)
-        w = 1.0 / (v @ v)
-        L += w * (r @ r)
-        g = -2.0 * w * apply_bsr_t(brow_ptr, bcol, A, r)
-        dP += np.einsum("ni,nj->nij", g.reshape(-1, 4), vn)
-    dC = (dP / s[:, None, None]).reshape(N, 16).astype(np.float32)
+    dW = np.zeros((N, 4, 4))
+    bj = lambda y: np.einsum("nij,nj->ni", Dinv, y.reshape(-1, 4)).ravel()
+    for i, w in enumerate(probes):
+        q = (w.reshape(-1, 4) * keep / sd).ravel()
+        v = apply_bsr(brow_ptr, bcol, A, bj(q)) if i % 2 == 1 else q
+        z = bj(v)
+        c = bj(v - apply_bsr(brow_ptr, bcol, A, z)).reshape(-1, 4) / sd
+        y = z + (sd * np.einsum("nij,nj->ni", W, c)).ravel()
+        r = (v - apply_bsr(brow_ptr, bcol, A, y)) * sd.ravel()
+        nv = np.sum((v * sd.ravel()) ** 2)
+        L += (r @ r) / nv
+        g = apply_bsr_t(brow_ptr, bcol, A, r * sd.ravel()).reshape(-1, 4) * sd
+        dW += (-2.0 / nv) * np.einsum("ni,nj->nij", g, c)
+    dC = (dW * keep[:, :, None] * keep[:, None, :]).reshape(N, 16).astype(np.float32)
     p = cache["p"]
     rows, off, deg = cache["rows"], cache["off"], cache["deg"]
     grads = {k: np.zeros_like(v, dtype=np.float32) for k, v in params.items()}

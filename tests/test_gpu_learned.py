@@ -5,10 +5,14 @@
   arithmetic, summation order differs: 1e-4 relative);
 * training on Jacobians the method produces (Newton systems of a J2 load step)
   lowers the loss;
-* on a held-out system the trained correction does not need more FGMRES
-  iterations than plain block-Jacobi (the gain is printed), converges to the
-  same 1e-10 relative residual, and the iteration cap falls back to plain
-  block-Jacobi.
+* on a held-out system (another mesh) the trained network needs fewer FGMRES
+  iterations than plain block-Jacobi, the method without it (the gain is
+  printed), converges to the same 1e-10 relative residual and solution, and
+  the iteration cap falls back to plain block-Jacobi.
+
+The meshes are Kuhn cubes with jittered interior nodes: on the exact grid the
+matrix inherits the grid's translation symmetry (repeated eigenvalues), which
+no mesh of a real part has.
 """
 import numpy as np
 import pytest
@@ -33,9 +37,9 @@ def bsr_host(d, s):
     return brow, bcol, diag, A
 
 
-def newton_system(n, steps):
+def newton_system(n, steps, seed=0):
     """The Newton system after ``steps`` J2 load steps (u_x = 0.001 t on x=1)."""
-    mesh = kuhn_cube(n)
+    mesh = kuhn_cube(n, jitter=0.2, seed=seed)
     d = api.Disc(mesh)
     m = api.Mechanics(d, api.J2, [MAT])
     s = api.SolInfo(d)
@@ -70,18 +74,18 @@ def test_forward_and_gradient_match_restatement():
     lo, go = M.loss_and_grad(theta, brow, bcol, diag, A, list(probes))
     assert abs(lg - lo) <= 1e-6 * abs(lo)
     assert np.linalg.norm(gg - go) <= 1e-4 * np.linalg.norm(go)
-    x, e, sv, Di = M.features(brow, bcol, diag, A)
+    x, e, sd, Di, dirichlet = M.features(brow, bcol, diag, A)
     Co = M.forward(M.unflatten(theta), brow, bcol, diag, x, e)
     C = net.corrections(s)
     assert np.abs(C - Co).max() <= 1e-4 * np.abs(Co).max()
 
 
 def test_training_and_gain_over_block_jacobi():
-    systems = [newton_system(8, k) for k in (1, 2, 3)]
+    systems = [newton_system(8, k, seed=k) for k in (1, 2, 3)]
     net = api.Learned(seed=0)
-    losses = net.train([x[2] for x in systems], epochs=40, lr=2e-3, num_probes=8)
-    assert losses[-1] < losses[0]
-    d, m, s, bcs = newton_system(10, 2)  # held out: another mesh
+    losses = net.train([x[2] for x in systems], epochs=60, lr=2e-3, num_probes=8)
+    assert losses[-1] < 0.5 * losses[0]
+    d, m, s, bcs = newton_system(10, 2, seed=99)  # held out: another mesh
     b = s.dMdu
     prm = dict(tolerance=1e-10, max_iters=20000, krylov_size=100)
     x0, plain = api.solve(s, b, params=api.solve_params(**prm))
@@ -89,7 +93,7 @@ def test_training_and_gain_over_block_jacobi():
     x1, learned = api.solve(s, b, params=api.solve_params(precond=api.PRECOND_LEARNED, **prm))
     print(f"\nFGMRES iterations to 1e-10: plain block-Jacobi {plain['iters']}, learned {learned['iters']}")
     assert plain["converged"] and learned["converged"]
-    assert learned["iters"] <= plain["iters"]
+    assert learned["iters"] < 0.8 * plain["iters"]
     assert np.linalg.norm(x1 - x0) <= 1e-7 * np.linalg.norm(x0)
     # cap: stop the learned run early and finish with plain block-Jacobi
     x2, capped = api.solve(s, b, params=api.solve_params(precond=api.PRECOND_LEARNED, learned_cap=5, **prm))
