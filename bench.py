@@ -232,17 +232,23 @@ def run_reference(a):
 
 
 # ------------------------------------------------------------------ adjoint leg
-def _j2_step(api, n, steps, max_newton=15):
-    """``steps`` J2 load steps of the stretched cube (u = 0 on x=0, u_x = 0.001 t
-    on x=1 at t = 1, 2, ...), the states updated between steps. One step of
-    0.002 is past what full Newton from zero converges in (the plastic front
-    jumps); two steps of 0.001 converge in a few iterations each."""
+LOAD_INC = 0.0005   # u_x increment per load step (yield strain Y/E = 0.00125)
+LOAD_STEPS = 3      # u_x = 0.0015 at the last step: the bar is plastic
+JITTER = 0.2
+
+
+def _j2_step(api, n, steps, seed=1, max_newton=15):
+    """``steps`` J2 load steps of the stretched cube (u = 0 on x=0, u_x =
+    LOAD_INC t on x=1 at t = 1, 2, ...), the states updated between steps, on a
+    Kuhn cube with jittered interior nodes (no grid symmetry). Full Newton
+    without line search (as goal's Primal::solve) needs increments of about
+    this size once the bar yields."""
     from goal_gb300.mesh import kuhn_cube
-    mesh = kuhn_cube(n)
+    mesh = kuhn_cube(n, jitter=JITTER, seed=seed)
     d = api.Disc(mesh)
     m = api.Mechanics(d, api.J2, [[MAT["E"], MAT["nu"], MAT["K"], MAT["Y"], MAT["c0"]]])
     s = api.SolInfo(d)
-    dbcs = [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", "0.001*t")]
+    dbcs = [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", f"{LOAD_INC}*t")]
     bcs = api.Bcs(d, dbcs, [])
     iters = []
     for k in range(1, steps + 1):
@@ -256,19 +262,22 @@ def _j2_step(api, n, steps, max_newton=15):
 
 
 def train_learned(api, epochs=60):
-    """Training data the method produces: Newton Jacobians of J2 load steps at
-    three load levels and the transposed Jacobian of a nested adjoint."""
+    """Training data the method produces: Newton Jacobians of the J2 load steps
+    (10^3 cubes, other jitter seeds) and the transposed Jacobian of a nested
+    adjoint (6^3 base cube)."""
     keep, systems = [], []
-    for steps in (1, 2, 3):
-        mesh, d, m, s, bcs, dbcs, _ = _j2_step(api, 10, steps)
+    for steps in range(1, LOAD_STEPS + 1):
+        mesh, d, m, s, bcs, dbcs, _ = _j2_step(api, 10, steps, seed=100 + steps)
         api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False)
         api.set_jac_dbcs(m, s, bcs, float(steps))
         keep.append((d, m, s, bcs))
         systems.append(s)
-    mesh, d, m, s, bcs, dbcs, _ = _j2_step(api, 6, 2)
+    mesh, d, m, s, bcs, dbcs, _ = _j2_step(api, 6, LOAD_STEPS, seed=200)
     na = api.NestedAdjoint(m, dbcs, [])
-    na.run(api.QOI_KS_VM, 20.0, 2.0, 1.0, api.solve_params(tolerance=1e-6, max_iters=50))
+    na.run(api.QOI_KS_VM, 20.0, float(LOAD_STEPS), float(LOAD_STEPS - 1),
+           api.solve_params(tolerance=1e-6, max_iters=50))
     keep.append((d, m, s, bcs, na))
+    systems.append(na.si_handle())
     net = api.Learned(seed=0)
     t0 = time.perf_counter()
     losses = net.train(systems, epochs=epochs, lr=2e-3, num_probes=8)
@@ -277,35 +286,38 @@ def train_learned(api, epochs=60):
 
 
 def adjoint_leg(n, api):
-    """Adjoint solve on the nested (uniformly refined) mesh after two J2 load
-    steps of the stretched cube (u_x = 0.001 t on x=1, t = 1, 2; u=0 on x=0): dRdu^T z = dM/du
-    with the KS von Mises functional (rho = 20), to 1e-10 relative residual with
-    plain FP64 block-Jacobi FGMRES, with FP32-inner / FP64-outer FGMRES, and with
-    the learned block-Jacobi correction inside the mixed solver; seconds and
-    iterations of each and the DWR estimates they give."""
+    """Adjoint solve on the nested (uniformly refined) mesh after the J2 load
+    steps of the stretched cube (u_x = LOAD_INC t on x=1, t = 1..LOAD_STEPS; u=0
+    on x=0): dRdu^T z = dM/du with the KS von Mises functional (rho = 20), to
+    1e-10 relative residual with plain FP64 block-Jacobi FGMRES, with the
+    learned correction in FP64, with FP32-inner / FP64-outer FGMRES, and with
+    the learned correction inside the mixed solver; seconds and iterations of
+    each and the DWR estimates they give."""
     t0 = time.perf_counter()
-    mesh, d, m, s, bcs, dbcs, newton = _j2_step(api, n, 2)
+    mesh, d, m, s, bcs, dbcs, newton = _j2_step(api, n, LOAD_STEPS)
     t_primal = time.perf_counter() - t0
     net, keep, train = train_learned(api)
     na = api.NestedAdjoint(m, dbcs, [])
     out = {"base_elements": mesh.num_elems, "nested_elements": na.disc.num_elems, "nested_dofs": na.disc.num_dofs,
+           "mesh": f"kuhn cube {n}^3 x 6 tets, interior nodes jittered by {JITTER} h, refined once",
            "newton_iters": newton["iters"], "primal_seconds": t_primal, "qoi": "KS von Mises rho=20",
            "tolerance": 1e-10, "training": train}
     runs = {"plain_fp64": api.solve_params(krylov_size=100, tolerance=1e-10, max_iters=30000),
+            "learned_fp64": api.solve_params(krylov_size=100, tolerance=1e-10, max_iters=30000,
+                                             precond=api.PRECOND_LEARNED, learned_cap=15000),
             "mixed": api.solve_params(krylov_size=30, tolerance=1e-10, max_iters=3000, precision=api.MIXED,
                                       inner_iters=30),
             "learned_mixed": api.solve_params(krylov_size=30, tolerance=1e-10, max_iters=3000, precision=api.MIXED,
                                               inner_iters=30, precond=api.PRECOND_LEARNED, learned_cap=1500)}
+    net.attach(na.si_handle())
     for name, prm in runs.items():
-        if name == "learned_mixed":
-            net.attach(na.si_handle())
-        r = na.run(api.QOI_KS_VM, 20.0, 2.0, 1.0, prm)
+        r = na.run(api.QOI_KS_VM, 20.0, float(LOAD_STEPS), float(LOAD_STEPS - 1), prm)
         out[name] = {"seconds": r["seconds_solve"], "iters": r["solve"]["iters"],
                      "inner_iters": r["solve"]["inner_iters"], "converged": r["solve"]["converged"],
                      "fell_back": r["solve"]["fell_back"], "rel_res": r["solve"]["rel_res"], "eta": r["eta"],
                      "bound": r["bound"]}
     p = out["plain_fp64"]
-    for k in ("mixed", "learned_mixed"):
+    for k in ("learned_fp64", "mixed", "learned_mixed"):
         q = out[k]
         out[f"speedup_{k}_vs_plain"] = p["seconds"] / q["seconds"] if q["seconds"] > 0 else None
         out[f"eta_rel_diff_{k}"] = abs(q["eta"] - p["eta"]) / max(abs(p["eta"]), 1e-300)
