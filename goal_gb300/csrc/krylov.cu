@@ -9,6 +9,8 @@
 
 #include "krylov.cuh"
 
+#include <type_traits>
+
 namespace goal {
 
 namespace {
@@ -25,6 +27,8 @@ struct GState {
 
 constexpr int kMaxM = 256;
 constexpr int kDotChunk = 8;
+constexpr int kRows = 8;               // rows per thread in the orthogonalization kernels
+constexpr int kSlab = 256 * kRows;     // rows per block
 
 template <typename T>
 struct Vec4;
@@ -43,31 +47,39 @@ struct Vec4<float> {
   }
 };
 
-// y = A x  (or y = b - A x). One warp per block row; lane = 4*slot + row.
+// Block-row product of node n, row r: sum_k A_k[r,:] . x_{bcol[k]}, one fused
+// multiply-add per matrix entry (on GB300 the FP64 pipe, not HBM, bounds the
+// FP64 kernels, so no operation is spent on reductions).
+template <typename T>
+__device__ __forceinline__ T block_row_dot(const int* __restrict__ bcol, const T* __restrict__ A,
+                                           const T* __restrict__ x, int b0, int b1, int r) {
+  T acc = T(0);
+#pragma unroll 4
+  for (int k = b0; k < b1; ++k) {
+    const int c = __ldg(bcol + k);
+    T a0, a1, a2, a3, x0, x1, x2, x3;
+    Vec4<T>::load(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+    Vec4<T>::load(x + 4ll * c, x0, x1, x2, x3);
+    acc = fma(a0, x0, acc);
+    acc = fma(a1, x1, acc);
+    acc = fma(a2, x2, acc);
+    acc = fma(a3, x3, acc);
+  }
+  return acc;
+}
+
+// y = A x  (or y = b - A x). Four threads per block row (one per row of the
+// node's 4x4 blocks), no cross-thread reduction.
 template <typename T, bool RESID>
 __global__ void __launch_bounds__(256) k_spmv(int N, const int* __restrict__ brow_ptr, const int* __restrict__ bcol,
                                               const T* __restrict__ A, const T* __restrict__ x,
                                               const T* __restrict__ b, T* __restrict__ y) {
-  const int lane = threadIdx.x & 31;
-  const int slot = lane >> 2, r = lane & 3;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += nw) {
-    const int b0 = __ldg(brow_ptr + n), b1 = __ldg(brow_ptr + n + 1);
-    T acc = T(0);
-    for (int k = b0 + slot; k < b1; k += 8) {
-      const int c = __ldg(bcol + k);
-      T a0, a1, a2, a3, x0, x1, x2, x3;
-      Vec4<T>::load(A + 16ll * k + 4 * r, a0, a1, a2, a3);
-      Vec4<T>::load(x + 4ll * c, x0, x1, x2, x3);
-      acc += a0 * x0 + a1 * x1 + a2 * x2 + a3 * x3;
-    }
-    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 8);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 16);
-    if (lane < 4) {
-      if (RESID) y[4ll * n + lane] = b[4ll * n + lane] - acc;
-      else y[4ll * n + lane] = acc;
-    }
+  const int r = threadIdx.x & 3;
+  const int nq = (gridDim.x * blockDim.x) >> 2;
+  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; n < N; n += nq) {
+    const T acc = block_row_dot(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
+    if (RESID) y[4ll * n + r] = b[4ll * n + r] - acc;
+    else y[4ll * n + r] = acc;
   }
 }
 
@@ -140,63 +152,73 @@ __global__ void __launch_bounds__(256) k_spmv_col(int N, const int* __restrict__
                                                   const T* Z, long long ld, const GState* st, T* __restrict__ y) {
   if (st->done) return;
   const T* x = Z + (long long)st->j * ld;
-  const int lane = threadIdx.x & 31;
-  const int slot = lane >> 2, r = lane & 3;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += nw) {
-    const int b0 = __ldg(brow_ptr + n), b1 = __ldg(brow_ptr + n + 1);
-    T acc = T(0);
-    for (int k = b0 + slot; k < b1; k += 8) {
-      const int c = __ldg(bcol + k);
-      T a0, a1, a2, a3, x0, x1, x2, x3;
-      Vec4<T>::load(A + 16ll * k + 4 * r, a0, a1, a2, a3);
-      Vec4<T>::load(x + 4ll * c, x0, x1, x2, x3);
-      acc += a0 * x0 + a1 * x1 + a2 * x2 + a3 * x3;
-    }
-    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 8);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 16);
-    if (lane < 4) y[4ll * n + lane] = acc;
-  }
+  const int r = threadIdx.x & 3;
+  const int nq = (gridDim.x * blockDim.x) >> 2;
+  for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; n < N; n += nq)
+    y[4ll * n + r] = block_row_dot(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
 }
 
-// partial dot products of w with columns 0..j of V and with itself (column j+1)
+// Orthogonalization kernels work on row slabs of kSlab = 256 x kRows rows per
+// block: every thread keeps its kRows entries of w in registers, and the
+// columns of V are streamed slab by slab (long contiguous reads, w read once).
+
+// Sums the kDotChunk per-thread values of a 256-thread block column by
+// column (staged through shared memory, one warp per column; no FP64 work for
+// float data); lane 0 of warp q returns column q's sum.
+template <typename T>
+__device__ __forceinline__ T chunk_reduce(const T (&acc)[kDotChunk], T (*sm)[257]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int cc = 0; cc < kDotChunk; ++cc) sm[cc][threadIdx.x] = acc[cc];
+  __syncthreads();
+  T v = T(0);
+#pragma unroll
+  for (int t = 0; t < 8; ++t) v += sm[wid][lane + 32 * t];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  return v;
+}
+
+// partial dot products of w with columns 0..j of V and with itself (column
+// j+1); part[c * gridDim.x + block]
 template <typename T>
 __global__ void __launch_bounds__(256) k_multidot(long long n, const T* V, long long ld, const T* __restrict__ w,
                                                   const GState* st, double* part, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
   const int j = st->j;
-  const int c0 = blockIdx.y * kDotChunk;
   const int ncols = j + 2;
-  if (c0 >= ncols) return;
-  T acc[kDotChunk];
+  const long long base = (long long)blockIdx.x * kSlab + threadIdx.x;
+  T wr[kRows];
 #pragma unroll
-  for (int q = 0; q < kDotChunk; ++q) acc[q] = T(0);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const T wi = w[i];
-#pragma unroll
-    for (int q = 0; q < kDotChunk; ++q) {
-      const int c = c0 + q;
-      if (c <= j) acc[q] += V[c * ld + i] * wi;
-      else if (c == j + 1) acc[q] += wi * wi;
-    }
+  for (int q = 0; q < kRows; ++q) {
+    const long long i = base + 256ll * q;
+    wr[q] = i < n ? w[i] : T(0);
   }
-  __shared__ double sm[kDotChunk][32];
+  __shared__ T sm[kDotChunk][257];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int c0 = 0; c0 < ncols; c0 += kDotChunk) {
+    T acc[kDotChunk];
 #pragma unroll
-  for (int q = 0; q < kDotChunk; ++q) {
-    double v = (double)acc[q];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sm[q][wid] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < kDotChunk) {
-    const int q = threadIdx.x;
-    double v = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) v += sm[q][k];
-    const int c = c0 + q;
-    if (c < ncols) part[(long long)c * gridDim.x + blockIdx.x] = v;
+    for (int cc = 0; cc < kDotChunk; ++cc) {
+      const int c = c0 + cc;
+      T a = T(0);
+      if (c <= j) {
+        const T* v = V + (long long)c * ld;
+#pragma unroll
+        for (int q = 0; q < kRows; ++q) {
+          const long long i = base + 256ll * q;
+          if (i < n) a = fma(v[i], wr[q], a);
+        }
+      } else if (c == j + 1) {
+#pragma unroll
+        for (int q = 0; q < kRows; ++q) a = fma(wr[q], wr[q], a);
+      }
+      acc[cc] = a;
+    }
+    const T v = chunk_reduce<T>(acc, sm);
+    const int c = c0 + wid;
+    if (lane == 0 && c < ncols) part[(long long)c * gridDim.x + blockIdx.x] = (double)v;
   }
 }
 
@@ -225,7 +247,7 @@ __global__ void k_dots_fin(int nbx, const double* part, GState* st, double* H, i
   }
 }
 
-// w -= V dots ; partial |w|^2
+// w -= V dots ; partial |w|^2 per block
 template <typename T>
 __global__ void __launch_bounds__(256) k_update(long long n, const T* V, long long ld, T* w, const double* dots,
                                                 const GState* st, double* part, int pass) {
@@ -235,22 +257,50 @@ __global__ void __launch_bounds__(256) k_update(long long n, const T* V, long lo
   __shared__ T sd[kMaxM + 1];
   for (int c = threadIdx.x; c <= j; c += blockDim.x) sd[c] = (T)dots[c];
   __syncthreads();
-  T acc = T(0);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    T v = w[i];
-    for (int c = 0; c <= j; ++c) v -= sd[c] * V[c * ld + i];
-    w[i] = v;
-    acc += v * v;
+  const long long base = (long long)blockIdx.x * kSlab + threadIdx.x;
+  T wr[kRows];
+#pragma unroll
+  for (int q = 0; q < kRows; ++q) {
+    const long long i = base + 256ll * q;
+    wr[q] = i < n ? w[i] : T(0);
   }
-  double a = (double)acc;
-  __shared__ double sm[32];
-  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
+  int c = 0;
+  for (; c + 1 <= j; c += 2) {
+    const T d0 = -sd[c], d1 = -sd[c + 1];
+    const T* v0 = V + (long long)c * ld;
+    const T* v1 = v0 + ld;
+#pragma unroll
+    for (int q = 0; q < kRows; ++q) {
+      const long long i = base + 256ll * q;
+      if (i < n) wr[q] = fma(d1, v1[i], fma(d0, v0[i], wr[q]));
+    }
+  }
+  for (; c <= j; ++c) {
+    const T d0 = -sd[c];
+    const T* v0 = V + (long long)c * ld;
+#pragma unroll
+    for (int q = 0; q < kRows; ++q) {
+      const long long i = base + 256ll * q;
+      if (i < n) wr[q] = fma(d0, v0[i], wr[q]);
+    }
+  }
+  T acc = T(0);
+#pragma unroll
+  for (int q = 0; q < kRows; ++q) {
+    const long long i = base + 256ll * q;
+    if (i < n) {
+      w[i] = wr[q];
+      acc = fma(wr[q], wr[q], acc);
+    }
+  }
+  __shared__ T sm[8];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
-    part[blockIdx.x] = s;
+    T s = T(0);
+    for (int k = 0; k < 8; ++k) s += sm[k];
+    part[blockIdx.x] = (double)s;
   }
 }
 
@@ -283,28 +333,41 @@ __global__ void k_normalize(long long n, T* V, long long ld, const T* w, const G
     v[i] = w[i] * inv;
 }
 
+// Applies the previous rotations to the new Hessenberg column (staged in
+// shared memory by the whole block), then forms rotation j (thread 0).
 __global__ void k_givens(GState* st, double* H, int ldh, double* cs, double* sn, double* g, int jmax, double tol_abs) {
   if (st->done) return;
   const int j = st->j;
   double* h = H + (long long)ldh * j;
-  for (int i = 0; i < j; ++i) {
-    double t = cs[i] * h[i] + sn[i] * h[i + 1];
-    h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
-    h[i] = t;
+  __shared__ double sh[kMaxM + 2], scs[kMaxM + 1], ssn[kMaxM + 1];
+  for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) sh[i] = h[i];
+  for (int i = threadIdx.x; i < j; i += blockDim.x) {
+    scs[i] = cs[i];
+    ssn[i] = sn[i];
   }
-  const double a = h[j], b = h[j + 1];
-  const double r = hypot(a, b);
-  double c = 1.0, s = 0.0;
-  if (r > 0.0) { c = a / r; s = b / r; }
-  cs[j] = c;
-  sn[j] = s;
-  h[j] = r;
-  h[j + 1] = 0.0;
-  g[j + 1] = -s * g[j];
-  g[j] = c * g[j];
-  st->res = fabs(g[j + 1]);
-  st->j = j + 1;
-  if (st->res <= tol_abs || st->j >= jmax || b == 0.0 || !(st->res == st->res)) st->done = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < j; ++i) {
+      const double t = scs[i] * sh[i] + ssn[i] * sh[i + 1];
+      sh[i + 1] = -ssn[i] * sh[i] + scs[i] * sh[i + 1];
+      sh[i] = t;
+    }
+    const double a = sh[j], b = sh[j + 1];
+    const double r = hypot(a, b);
+    double c = 1.0, s = 0.0;
+    if (r > 0.0) { c = a / r; s = b / r; }
+    cs[j] = c;
+    sn[j] = s;
+    sh[j] = r;
+    sh[j + 1] = 0.0;
+    g[j + 1] = -s * g[j];
+    g[j] = c * g[j];
+    st->res = fabs(g[j + 1]);
+    st->j = j + 1;
+    if (st->res <= tol_abs || st->j >= jmax || b == 0.0 || !(st->res == st->res)) st->done = 1;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) h[i] = sh[i];
 }
 
 __global__ void k_backsolve(const GState* st, const double* H, int ldh, const double* g, double* y) {
@@ -323,28 +386,28 @@ __global__ void k_combine(long long n, const T* Z, long long ld, const double* y
   __shared__ double sy[kMaxM];
   for (int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = y[c];
   __syncthreads();
+  // FP64 results accumulate in FP64; an FP32 result (the inner solve) in FP32
+  using Acc = typename std::conditional<std::is_same<TX, float>::value, float, double>::type;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double s = zero_first ? 0.0 : (double)x[i];
-    for (int c = 0; c < k; ++c) s += sy[c] * (double)Z[c * ld + i];
+    Acc s = zero_first ? Acc(0) : (Acc)x[i];
+    for (int c = 0; c < k; ++c) s = fma((Acc)sy[c], (Acc)Z[c * ld + i], s);
     x[i] = (TX)s;
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_norm2_part(long long n, const T* x, double* part) {
-  double a = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double v = (double)x[i];
-    a += v * v;
-  }
-  __shared__ double sm[32];
+  T a = T(0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a = fma(x[i], x[i], a);
+  __shared__ T sm[32];
   for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
+    T s = T(0);
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
-    part[blockIdx.x] = s;
+    part[blockIdx.x] = (double)s;
   }
 }
 
@@ -374,9 +437,9 @@ __global__ void k_cycle_fin(int nbx, const double* part, GState* st, double* g, 
 template <typename T, typename TR>
 __global__ void k_scale_into(long long n, const TR* r, const GState* st, T* v0) {
   const double beta = st->beta;
-  const double inv = beta > 0.0 ? 1.0 / beta : 0.0;
+  const T inv = (T)(beta > 0.0 ? 1.0 / beta : 0.0);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    v0[i] = (T)((double)r[i] * inv);
+    v0[i] = (T)r[i] * inv;
 }
 
 __global__ void k_col_to_f32(long long n, const double* V, long long ld, const GState* st, float* out) {
@@ -464,8 +527,9 @@ __global__ void k_to_f32(long long n, const double* in, float* out) {
     out[i] = (float)in[i];
 }
 
-int spmv_grid(int N) { return grid_for((long long)N * 32, 256, kSMs * 16); }
+int spmv_grid(int N) { return grid_for((long long)N * 4, 256, kSMs * 16); }
 int vec_grid(long long n) { return grid_for(n, 256, kSMs * 8); }
+int slab_grid(long long n) { return (int)std::max(1ll, (n + kSlab - 1) / kSlab); }
 
 }  // namespace
 
@@ -486,7 +550,7 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
   need(sn, m_ + 1);
   need(g, m_ + 2);
   need(y, m_ + 1);
-  need(red, (size_t)(kMaxM + 4) * kSMs * 8);
+  need(red, (size_t)(kMaxM + 4) * std::max(kSMs * 8, slab_grid(n_)));
   need(scal, 64);
   need(flag, 8);
   need(dots, kMaxM + 2);
@@ -544,12 +608,11 @@ namespace {
 template <typename T>
 void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, double* cs, double* sn, double* g,
                   double* dots, double* red, int jmax, double tol_abs, cudaStream_t s) {
-  const int nbx = vec_grid(n);
-  const int nchunks = (jmax + 2 + kDotChunk - 1) / kDotChunk;
+  const int nbx = slab_grid(n);
   double* part = red;
   double* npart = red + (size_t)(kMaxM + 2) * nbx;
   for (int pass = 0; pass < 2; ++pass) {
-    k_multidot<T><<<dim3(nbx, nchunks), 256, 0, s>>>(n, V, n, w, st, part, pass);
+    k_multidot<T><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
     GOAL_CHECK_LAUNCH();
     k_dots_fin<<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
     GOAL_CHECK_LAUNCH();
@@ -560,7 +623,7 @@ void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, doubl
   }
   k_normalize<T><<<nbx, 256, 0, s>>>(n, V, n, w, st, H, ldh);
   GOAL_CHECK_LAUNCH();
-  k_givens<<<1, 1, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
+  k_givens<<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
   GOAL_CHECK_LAUNCH();
 }
 
