@@ -188,6 +188,19 @@ extern "C" {
 
 const char* goal_last_error(void) { return t_last_error.c_str(); }
 
+int goal_assembly_timing(int enable) {
+  GOAL_API_BEGIN
+  goal::assembly_timing(enable != 0);
+  GOAL_API_END
+}
+
+int goal_assembly_timing_read(double* ms, long long* count) {
+  GOAL_API_BEGIN
+  GOAL_ARG(ms && count, "null argument");
+  goal::assembly_timing_read(ms, count);
+  GOAL_API_END
+}
+
 long long goal_launch_count(void) { return g_launches.load(); }
 
 int goal_eval(const char* expr, double x, double y, double z, double t, double* out) {

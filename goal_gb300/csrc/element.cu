@@ -781,6 +781,34 @@ void ks_prepass(Mechanics& m, double rho, double& max_vm, double& scale, cudaStr
   scale = device_sum(m.qoi_elem.ptr, E, m.red, st);
 }
 
+namespace {
+// Optional device timing of the two assembly phases (CUDA events on the
+// assembly's stream, read after the stream synchronisation that ends every
+// assembly). Off unless enabled.
+struct PhaseTimer {
+  bool on = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  double elem_ms = 0.0, gather_ms = 0.0;
+  long long count = 0;
+} g_phase;
+}  // namespace
+
+void assembly_timing(bool enable) {
+  if (enable && !g_phase.ev[0])
+    for (auto& e : g_phase.ev) GOAL_CUDA(cudaEventCreate(&e));
+  g_phase.on = enable;
+  if (enable) {
+    g_phase.elem_ms = g_phase.gather_ms = 0.0;
+    g_phase.count = 0;
+  }
+}
+
+void assembly_timing_read(double* ms, long long* count) {
+  ms[0] = g_phase.elem_ms;
+  ms[1] = g_phase.gather_ms;
+  *count = g_phase.count;
+}
+
 double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w, cudaStream_t st) {
   const Disc& d = *m.disc;
   ElemArgs a;
@@ -837,8 +865,11 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
       a.dbuf = m.dbuf.ptr;
     }
   }
+  const bool timed = g_phase.on;
+  if (timed) GOAL_CUDA(cudaEventRecord(g_phase.ev[0], st));
   if (m.model == MODEL_J2) dispatch<MODEL_J2>(d, c, a, st, buf);
   else dispatch<MODEL_NEOHOOKEAN>(d, c, a, st, buf);
+  if (timed) GOAL_CUDA(cudaEventRecord(g_phase.ev[1], st));
   if (buf && scatter) {
     const int acc = c.overwrite ? 0 : 1;
     k_gather_nodes<<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(d.num_nodes, d.nptr.ptr, d.nlist.ptr,
@@ -859,6 +890,7 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
                                                                         16, s->dMdu.ptr, c.overwrite ? 0 : 1);
     GOAL_CHECK_LAUNCH();
   }
+  if (timed) GOAL_CUDA(cudaEventRecord(g_phase.ev[2], st));
   int hstat = 0;
   GOAL_CUDA(cudaMemcpyAsync(&hstat, m.status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
   double q = 0.0;
@@ -867,6 +899,14 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
     if (c.qoi == QOI_KS_VM) q = ks_max + (1.0 / c.rho) * std::log(ks_scale);
   } else {
     GOAL_CUDA(cudaStreamSynchronize(st));
+  }
+  if (timed) {
+    float e = 0.0f, g = 0.0f;
+    GOAL_CUDA(cudaEventElapsedTime(&e, g_phase.ev[0], g_phase.ev[1]));
+    GOAL_CUDA(cudaEventElapsedTime(&g, g_phase.ev[1], g_phase.ev[2]));
+    g_phase.elem_ms += e;
+    g_phase.gather_ms += g;
+    g_phase.count += 1;
   }
   GOAL_REQUIRE(hstat == 0, GOAL_ERR_RETURN_MAP, "J2: return mapping failed");
   return q;

@@ -73,6 +73,10 @@ struct ErrorWeights {
 // assemble(E, SolInfo*) (src/goal_assembly.cpp:65-88) for one chain.
 // Returns the QoI value when chain.qoi != QOI_NONE.
 double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w, cudaStream_t stream);
+// Device time of the element-kernel phase and of the gather phase of every
+// assemble() while enabled (enable clears the sums).
+void assembly_timing(bool enable);
+void assembly_timing_read(double* ms, long long* count);
 
 // KS pre-pass over stored stresses (src/goal_ks_vm.cpp:36-76): max von Mises and scale.
 void ks_prepass(Mechanics& m, double rho, double& max_vm, double& scale, cudaStream_t stream);

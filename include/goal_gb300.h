@@ -156,6 +156,12 @@ typedef struct {
   int colored; /* 0: element buffer + deterministic gather (default); 1: colour-by-colour in place */
 } goal_chain;
 int goal_assemble(goal_mechanics m, goal_sol_info s, const goal_chain* chain, double* qoi_value);
+/* No counterpart in the reference. Device time of goal_assemble's two phases,
+ * measured with CUDA events on the discretization's stream: enable != 0 clears
+ * the sums and starts measuring, 0 stops. ms[0] = element kernel(s), ms[1] =
+ * gathers of R, dMdu and the matrix blocks; count = assemblies measured. */
+int goal_assembly_timing(int enable);
+int goal_assembly_timing_read(double* ms, long long* count);
 
 /* ---------------------------------------------------------------- boundary conditions
  * "dirichlet bcs: [eq, node set, expr]" and "traction bcs: [side set, Tx, Ty, Tz]". */
