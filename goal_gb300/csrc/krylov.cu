@@ -27,8 +27,7 @@ struct GState {
 
 constexpr int kMaxM = 256;
 constexpr int kDotChunk = 8;
-constexpr int kRows = 8;               // rows per thread in the orthogonalization kernels
-constexpr int kSlab = 256 * kRows;     // rows per block
+constexpr int kMaxRows = 8;  // rows per thread in the orthogonalization kernels: 1, 2, 4 or 8
 
 template <typename T>
 struct Vec4;
@@ -158,8 +157,8 @@ __global__ void __launch_bounds__(256) k_spmv_col(int N, const int* __restrict__
     y[4ll * n + r] = block_row_dot(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
 }
 
-// Orthogonalization kernels work on row slabs of kSlab = 256 x kRows rows per
-// block: every thread keeps its kRows entries of w in registers, and the
+// Orthogonalization kernels work on row slabs of 256 x R rows per block:
+// every thread keeps its R entries of w in registers, and the
 // columns of V are streamed slab by slab (long contiguous reads, w read once).
 
 // Sums the kDotChunk per-thread values of a 256-thread block column by
@@ -181,17 +180,17 @@ __device__ __forceinline__ T chunk_reduce(const T (&acc)[kDotChunk], T (*sm)[257
 
 // partial dot products of w with columns 0..j of V and with itself (column
 // j+1); part[c * gridDim.x + block]
-template <typename T>
+template <typename T, int R>
 __global__ void __launch_bounds__(256) k_multidot(long long n, const T* V, long long ld, const T* __restrict__ w,
                                                   const GState* st, double* part, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
   const int j = st->j;
   const int ncols = j + 2;
-  const long long base = (long long)blockIdx.x * kSlab + threadIdx.x;
-  T wr[kRows];
+  const long long base = (long long)blockIdx.x * (256ll * R) + threadIdx.x;
+  T wr[R];
 #pragma unroll
-  for (int q = 0; q < kRows; ++q) {
+  for (int q = 0; q < R; ++q) {
     const long long i = base + 256ll * q;
     wr[q] = i < n ? w[i] : T(0);
   }
@@ -206,13 +205,13 @@ __global__ void __launch_bounds__(256) k_multidot(long long n, const T* V, long 
       if (c <= j) {
         const T* v = V + (long long)c * ld;
 #pragma unroll
-        for (int q = 0; q < kRows; ++q) {
+        for (int q = 0; q < R; ++q) {
           const long long i = base + 256ll * q;
           if (i < n) a = fma(v[i], wr[q], a);
         }
       } else if (c == j + 1) {
 #pragma unroll
-        for (int q = 0; q < kRows; ++q) a = fma(wr[q], wr[q], a);
+        for (int q = 0; q < R; ++q) a = fma(wr[q], wr[q], a);
       }
       acc[cc] = a;
     }
@@ -248,7 +247,7 @@ __global__ void k_dots_fin(int nbx, const double* part, GState* st, double* H, i
 }
 
 // w -= V dots ; partial |w|^2 per block
-template <typename T>
+template <typename T, int R>
 __global__ void __launch_bounds__(256) k_update(long long n, const T* V, long long ld, T* w, const double* dots,
                                                 const GState* st, double* part, int pass) {
   if (st->done) return;
@@ -257,10 +256,10 @@ __global__ void __launch_bounds__(256) k_update(long long n, const T* V, long lo
   __shared__ T sd[kMaxM + 1];
   for (int c = threadIdx.x; c <= j; c += blockDim.x) sd[c] = (T)dots[c];
   __syncthreads();
-  const long long base = (long long)blockIdx.x * kSlab + threadIdx.x;
-  T wr[kRows];
+  const long long base = (long long)blockIdx.x * (256ll * R) + threadIdx.x;
+  T wr[R];
 #pragma unroll
-  for (int q = 0; q < kRows; ++q) {
+  for (int q = 0; q < R; ++q) {
     const long long i = base + 256ll * q;
     wr[q] = i < n ? w[i] : T(0);
   }
@@ -270,7 +269,7 @@ __global__ void __launch_bounds__(256) k_update(long long n, const T* V, long lo
     const T* v0 = V + (long long)c * ld;
     const T* v1 = v0 + ld;
 #pragma unroll
-    for (int q = 0; q < kRows; ++q) {
+    for (int q = 0; q < R; ++q) {
       const long long i = base + 256ll * q;
       if (i < n) wr[q] = fma(d1, v1[i], fma(d0, v0[i], wr[q]));
     }
@@ -279,14 +278,14 @@ __global__ void __launch_bounds__(256) k_update(long long n, const T* V, long lo
     const T d0 = -sd[c];
     const T* v0 = V + (long long)c * ld;
 #pragma unroll
-    for (int q = 0; q < kRows; ++q) {
+    for (int q = 0; q < R; ++q) {
       const long long i = base + 256ll * q;
       if (i < n) wr[q] = fma(d0, v0[i], wr[q]);
     }
   }
   T acc = T(0);
 #pragma unroll
-  for (int q = 0; q < kRows; ++q) {
+  for (int q = 0; q < R; ++q) {
     const long long i = base + 256ll * q;
     if (i < n) {
       w[i] = wr[q];
@@ -529,7 +528,17 @@ __global__ void k_to_f32(long long n, const double* in, float* out) {
 
 int spmv_grid(int N) { return grid_for((long long)N * 4, 256, kSMs * 16); }
 int vec_grid(long long n) { return grid_for(n, 256, kSMs * 8); }
-int slab_grid(long long n) { return (int)std::max(1ll, (n + kSlab - 1) / kSlab); }
+// Rows per thread of the orthogonalization kernels: enough blocks to fill the
+// GPU (8 per SM for FP32, 4 per SM for FP64, whose reductions cost FP64
+// instructions and so want longer slabs), at most kMaxRows.
+template <typename T>
+int slab_rows(long long n) {
+  const long long target = (std::is_same<T, float>::value ? 8ll : 4ll) * kSMs * 256;
+  int r = 1;
+  while (r < kMaxRows && n >= 2ll * r * target) r *= 2;
+  return r;
+}
+int slab_grid(long long n, int rows) { return (int)std::max(1ll, (n + 256ll * rows - 1) / (256ll * rows)); }
 
 }  // namespace
 
@@ -550,7 +559,7 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
   need(sn, m_ + 1);
   need(g, m_ + 2);
   need(y, m_ + 1);
-  need(red, (size_t)(kMaxM + 4) * std::max(kSMs * 8, slab_grid(n_)));
+  need(red, (size_t)(kMaxM + 4) * std::max(kSMs * 8, slab_grid(n_, 1)));
   need(scal, 64);
   need(flag, 8);
   need(dots, kMaxM + 2);
@@ -603,25 +612,38 @@ void spmv32(const BsrView& A, const float* vals, const float* x, float* y, cudaS
 
 namespace {
 
+// Classical Gram-Schmidt of w against V_0..V_j, with a second pass when the
+// first one removed more than half of |w|^2 (device-side decision).
+template <typename T, int R>
+void orth_passes(long long n, T* V, T* w, GState* st, double* H, int ldh, double* dots, double* red, int jmax,
+                 cudaStream_t s) {
+  const int nbx = slab_grid(n, R);
+  double* part = red;
+  double* npart = red + (size_t)(kMaxM + 2) * nbx;
+  for (int pass = 0; pass < 2; ++pass) {
+    k_multidot<T, R><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
+    GOAL_CHECK_LAUNCH();
+    k_dots_fin<<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
+    GOAL_CHECK_LAUNCH();
+    k_update<T, R><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
+    GOAL_CHECK_LAUNCH();
+    k_norm_fin<<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
+    GOAL_CHECK_LAUNCH();
+  }
+}
+
 // One Arnoldi step's orthogonalization (CGS with a conditional second pass),
 // normalization and Givens update, on state st.
 template <typename T>
 void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, double* cs, double* sn, double* g,
                   double* dots, double* red, int jmax, double tol_abs, cudaStream_t s) {
-  const int nbx = slab_grid(n);
-  double* part = red;
-  double* npart = red + (size_t)(kMaxM + 2) * nbx;
-  for (int pass = 0; pass < 2; ++pass) {
-    k_multidot<T><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
-    GOAL_CHECK_LAUNCH();
-    k_dots_fin<<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
-    GOAL_CHECK_LAUNCH();
-    k_update<T><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
-    GOAL_CHECK_LAUNCH();
-    k_norm_fin<<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
-    GOAL_CHECK_LAUNCH();
+  switch (slab_rows<T>(n)) {
+    case 1: orth_passes<T, 1>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
+    case 2: orth_passes<T, 2>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
+    case 4: orth_passes<T, 4>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
+    default: orth_passes<T, 8>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
   }
-  k_normalize<T><<<nbx, 256, 0, s>>>(n, V, n, w, st, H, ldh);
+  k_normalize<T><<<vec_grid(n), 256, 0, s>>>(n, V, n, w, st, H, ldh);
   GOAL_CHECK_LAUNCH();
   k_givens<<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
   GOAL_CHECK_LAUNCH();
@@ -639,6 +661,41 @@ double read_norm(long long n, const double* x, Krylov& K) {
   return K.h_scal[0];
 }
 
+}  // namespace
+
+namespace {
+// A captured CUDA graph, instantiated once and destroyed with its owner. The
+// launch counter counts the captured kernels each time the graph runs.
+struct StepGraph {
+  cudaGraphExec_t exec = nullptr;
+  long long kernels = 0;
+  template <class F>
+  void capture(cudaStream_t s, F&& issue) {
+    cudaGraph_t g = nullptr;
+    const long long before = g_launches.load();
+    GOAL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      issue();
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    GOAL_CUDA(cudaStreamEndCapture(s, &g));
+    kernels = g_launches.load() - before;
+    g_launches.fetch_sub(kernels);
+    cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    GOAL_CUDA(e);
+  }
+  void launch(cudaStream_t s) {
+    GOAL_CUDA(cudaGraphLaunch(exec, s));
+    g_launches.fetch_add(kernels);
+  }
+  ~StepGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
 }  // namespace
 
 SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double* x, const SolveParams& p, Krylov& K) {
@@ -674,6 +731,78 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
   double beta = read_norm(n, K.r.ptr, K);
   out.rel_res = bnorm > 0 ? beta / bnorm : beta;
   const int nbx = vec_grid(n);
+  const bool sweep2 = K.two_sweep;
+
+  // One outer Arnoldi step: Z_j = M^-1 V_j, w = A Z_j, orthogonalization and
+  // Givens update. Every kernel is gated on the outer state.
+  auto issue_step = [&]() {
+    if (!mixed) {
+      k_bj_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv.ptr, K.V.ptr, K.Z.ptr, n, st);
+      GOAL_CHECK_LAUNCH();
+      if (sweep2) {
+        k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
+        GOAL_CHECK_LAUNCH();
+        k_second_sweep_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc.ptr, K.V.ptr, n, K.w.ptr, K.Z.ptr, n, st);
+        GOAL_CHECK_LAUNCH();
+      }
+    } else {
+      // inner FP32 GMRES on A32 with the right preconditioner, fixed mi
+      // iterations: Z_j = M^-1 V32 y with V32 the inner basis started from V_j
+      k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.r32.ptr);
+      GOAL_CHECK_LAUNCH();
+      k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.red.ptr);
+      GOAL_CHECK_LAUNCH();
+      k_cycle_fin<<<1, 256, 0, s>>>(nbx, K.red.ptr, sti, gin, mi, nullptr);
+      GOAL_CHECK_LAUNCH();
+      k_gate<<<1, 1, 0, s>>>(st, sti);
+      GOAL_CHECK_LAUNCH();
+      k_scale_into<float, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V32.ptr);
+      GOAL_CHECK_LAUNCH();
+      for (int it = 0; it < mi; ++it) {
+        // r32 = M^-1 v_it ; w32 = A32 r32 (ld 0 keeps the input at r32)
+        k_bj_colin<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V32.ptr, n, sti, K.r32.ptr);
+        GOAL_CHECK_LAUNCH();
+        if (sweep2) {
+          k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
+                                                         K.t32.ptr);
+          GOAL_CHECK_LAUNCH();
+          k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V32.ptr, n, K.t32.ptr,
+                                                                     K.r32.ptr, 0, sti);
+          GOAL_CHECK_LAUNCH();
+        }
+        k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
+                                                       K.w32.ptr);
+        GOAL_CHECK_LAUNCH();
+        arnoldi_orth<float>(n, K.V32.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0, s);
+      }
+      k_backsolve<<<1, 1, 0, s>>>(sti, Hin, mi + 1, gin, yin);
+      GOAL_CHECK_LAUNCH();
+      k_combine<float, float><<<nbx, 256, 0, s>>>(n, K.V32.ptr, n, yin, sti, K.w32.ptr, 1);
+      GOAL_CHECK_LAUNCH();
+      k_bj<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.w32.ptr, K.r32.ptr);
+      GOAL_CHECK_LAUNCH();
+      if (sweep2) {
+        k_spmv<float, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, nullptr,
+                                                          K.t32.ptr);
+        GOAL_CHECK_LAUNCH();
+        k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.w32.ptr, 0, K.t32.ptr,
+                                                                   K.r32.ptr, 0, nullptr);
+        GOAL_CHECK_LAUNCH();
+      }
+      k_f32_to_col<<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.Z.ptr, n, st);
+      GOAL_CHECK_LAUNCH();
+    }
+    k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
+    GOAL_CHECK_LAUNCH();
+    arnoldi_orth<double>(n, K.V.ptr, K.w.ptr, st, K.H.ptr, m + 1, K.cs.ptr, K.sn.ptr, K.g.ptr, dots, K.red.ptr, m,
+                         tol_abs, s);
+  };
+  // one Arnoldi step as a CUDA graph, captured once per solve; its kernels are
+  // gated on the device state, so steps launched past the end of a cycle are
+  // no-ops, and the host reads the state every `batch` steps
+  StepGraph step_graph;
+  const int batch = mixed ? 1 : 4;
+
   while (beta > tol_abs && out.iters < p.max_iters) {
     // start a cycle: V_0 = r / beta
     k_norm2_part<double><<<nbx, 256, 0, s>>>(n, K.r.ptr, K.red.ptr);
@@ -683,79 +812,25 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
     k_scale_into<double, double><<<nbx, 256, 0, s>>>(n, K.r.ptr, st, K.V.ptr);
     GOAL_CHECK_LAUNCH();
     const int steps = std::min(m, p.max_iters - out.iters);
+    if (!step_graph.exec) step_graph.capture(s, issue_step);
     int done_steps = 0;
-    for (int step = 0; step < steps; ++step) {
-      if (!mixed) {
-        k_bj_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv.ptr, K.V.ptr, K.Z.ptr, n, st);
-        GOAL_CHECK_LAUNCH();
-        if (K.two_sweep) {
-          k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
-          GOAL_CHECK_LAUNCH();
-          k_second_sweep_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc.ptr, K.V.ptr, n, K.w.ptr, K.Z.ptr, n, st);
-          GOAL_CHECK_LAUNCH();
-          out.spmv64++;
-        }
-      } else {
-        // inner FP32 GMRES on A32 with right block-Jacobi, fixed mi iterations:
-        // Z_j = M^-1 V32 y with V32 the inner basis started from V_j
-        k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.r32.ptr);
-        GOAL_CHECK_LAUNCH();
-        k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.red.ptr);
-        GOAL_CHECK_LAUNCH();
-        k_cycle_fin<<<1, 256, 0, s>>>(nbx, K.red.ptr, sti, gin, mi, nullptr);
-        GOAL_CHECK_LAUNCH();
-        k_gate<<<1, 1, 0, s>>>(st, sti);
-        GOAL_CHECK_LAUNCH();
-        k_scale_into<float, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V32.ptr);
-        GOAL_CHECK_LAUNCH();
-        for (int it = 0; it < mi; ++it) {
-          k_bj_colin<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V32.ptr, n, sti, K.r32.ptr);
-          GOAL_CHECK_LAUNCH();
-          if (K.two_sweep) {
-            k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
-                                                           K.t32.ptr);
-            GOAL_CHECK_LAUNCH();
-            k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V32.ptr, n, K.t32.ptr,
-                                                                       K.r32.ptr, 0, sti);
-            GOAL_CHECK_LAUNCH();
-            out.spmv32++;
-          }
-          // r32 = M^-1 v_it ; w32 = A32 r32 (ld 0 keeps the input at r32)
-          k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
-                                                         K.w32.ptr);
-          GOAL_CHECK_LAUNCH();
-          arnoldi_orth<float>(n, K.V32.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0, s);
-        }
-        k_backsolve<<<1, 1, 0, s>>>(sti, Hin, mi + 1, gin, yin);
-        GOAL_CHECK_LAUNCH();
-        k_combine<float, float><<<nbx, 256, 0, s>>>(n, K.V32.ptr, n, yin, sti, K.w32.ptr, 1);
-        GOAL_CHECK_LAUNCH();
-        k_bj<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.w32.ptr, K.r32.ptr);
-        GOAL_CHECK_LAUNCH();
-        if (K.two_sweep) {
-          k_spmv<float, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, nullptr,
-                                                            K.t32.ptr);
-          GOAL_CHECK_LAUNCH();
-          k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.w32.ptr, 0, K.t32.ptr,
-                                                                     K.r32.ptr, 0, nullptr);
-          GOAL_CHECK_LAUNCH();
-          out.spmv32++;
-        }
-        k_f32_to_col<<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.Z.ptr, n, st);
-        GOAL_CHECK_LAUNCH();
-        out.inner_iters += mi;
-        out.spmv32 += mi;
-      }
-      k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
-      GOAL_CHECK_LAUNCH();
-      out.spmv64++;
-      arnoldi_orth<double>(n, K.V.ptr, K.w.ptr, st, K.H.ptr, m + 1, K.cs.ptr, K.sn.ptr, K.g.ptr, dots, K.red.ptr, m,
-                           tol_abs, s);
+    for (int step = 0; step < steps;) {
+      const int k = std::min(batch, steps - step);
+      for (int q = 0; q < k; ++q) step_graph.launch(s);
+      step += k;
       GOAL_CUDA(cudaMemcpyAsync(K.h_scal, K.scal.ptr, sizeof(GState), cudaMemcpyDeviceToHost, s));
       GOAL_CUDA(cudaStreamSynchronize(s));
       const GState* hs = reinterpret_cast<const GState*>(K.h_scal);
       done_steps = hs->j;
       if (hs->done) break;
+    }
+    const long long extra = sweep2 ? 1 : 0;
+    if (mixed) {
+      out.inner_iters += (long long)mi * done_steps;
+      out.spmv32 += (long long)done_steps * (mi * (1 + extra) + extra);
+      out.spmv64 += done_steps;
+    } else {
+      out.spmv64 += (long long)done_steps * (1 + extra);
     }
     out.iters += done_steps;
     k_backsolve<<<1, 1, 0, s>>>(st, K.H.ptr, m + 1, K.g.ptr, K.y.ptr);
