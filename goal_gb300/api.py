@@ -439,3 +439,14 @@ class Learned:
             self.close()
         except Exception:
             pass
+
+
+def size_field(disc: Disc, elem_error, target: int) -> np.ndarray:
+    """get_iso_target_size (src/goal_size_field.cpp:139-151): per-node target
+    sizes from per-element error indicators and a target element count."""
+    err = _f64(elem_error)
+    if err.shape != (disc.num_elems,):
+        raise ValueError("one error indicator per element")
+    out = np.zeros(disc.num_nodes)
+    check(lib().goal_size_field(disc.h, _ptr(err), int(target), _ptr(out)))
+    return out

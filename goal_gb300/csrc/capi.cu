@@ -8,6 +8,7 @@
 #include "capi_internal.cuh"
 #include "driver.cuh"
 #include "mpnn.cuh"
+#include "size_field.cuh"
 
 namespace goal {
 
@@ -333,6 +334,20 @@ int goal_nested_create(goal_disc base, goal_disc* out) {
   h->d = refine_uniform(*base->d);
   h->owns_stream = false;
   *out = h.release();
+  GOAL_API_END
+}
+
+int goal_size_field(goal_disc d, const double* elem_error, int target, double* vtx_size) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && elem_error && vtx_size && d->d->built, "goal_size_field: null argument or disc not built");
+  GOAL_ARG(target > 0, "goal_size_field: target elements must be positive");
+  Disc& D = *d->d;
+  DevBuf<double> err, out;
+  err.upload(elem_error, D.num_elems, D.stream);
+  out.alloc(D.num_nodes);
+  iso_target_size(D, err.ptr, target, out.ptr, D.stream);
+  out.download(vtx_size, D.stream);
+  GOAL_CUDA(cudaStreamSynchronize(D.stream));
   GOAL_API_END
 }
 

@@ -101,6 +101,15 @@ int goal_nested_create(goal_disc base, goal_disc* out);
 /* end points of the edge of every new node: edges[2*(n - base_nodes) + {0,1}] */
 int goal_nested_parent_edges(goal_disc nested, int* edges);
 
+/* get_iso_target_size (src/goal_size_field.cpp:139-151): the isotropic target
+ * size field that drives goal's mesh adaptation, from per-element error
+ * indicators (elem_error[num_elems], caller's element order; e.g. the base
+ * indicators of goal_nested_adjoint_run) and a target element count. Writes
+ * one size per node (vtx_size[num_nodes]): the mean over the node's elements
+ * of (G/target)^(1/3) |e|^(-2/5) h_e clamped to [h_e/4, 2 h_e], with
+ * G = sum |e|^(6/5) and h_e the root mean square edge length. */
+int goal_size_field(goal_disc d, const double* elem_error, int target, double* vtx_size);
+
 /* ---------------------------------------------------------------- Mechanics
  * goal::create_mechanics (src/goal_mechanics.hpp:50). materials holds, per
  * element set, E, nu, K, Y, c0 (K and Y are read by J2 only). States start as

@@ -72,9 +72,10 @@ def test_yaml_lite_parses_reference_layout():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["neohookean_uniaxial_3D", "J2_traction_3D"])
-def test_cli_primal_regression(case, tmp_path):
+def test_cli_primal_regression(case, tmp_path, monkeypatch):
     import shutil
     from goal_gb300 import cli
+    monkeypatch.chdir(tmp_path)
     c = _cases()[case]
     shutil.copy(os.path.join(ROOT, "tests", "golden", "cube_mesh.npz"), tmp_path / "cube.npz")
     y = tmp_path / "input.yaml"
@@ -84,3 +85,66 @@ def test_cli_primal_regression(case, tmp_path):
     assert abs(J - c["value"]) < c["tolerance"]
     assert any(l.startswith(" > J(uH) = ") for l in lines)
     assert any("regression" in l for l in lines)
+
+
+def _with_output(text, **opts):
+    extra = "".join(f"    {k}: {v}\n" for k, v in opts.items())
+    return text.replace("  output:\n", "  output:\n" + extra)
+
+
+@pytest.mark.gpu
+def test_cli_output_and_restart(tmp_path, monkeypatch):
+    """Three J2 load steps in one run equal two steps, a native restart and
+    the third step; every step writes a ParaView dataset."""
+    import shutil
+    import xml.etree.ElementTree as ET
+    from goal_gb300 import cli
+    monkeypatch.chdir(tmp_path)
+    case = "J2_uniaxial_3D"
+    c = dict(_cases()[case])
+    shutil.copy(os.path.join(ROOT, "tests", "golden", "cube_mesh.npz"), tmp_path / "cube.npz")
+    full = tmp_path / "full.yaml"
+    full.write_text(reference_style_yaml(case, c, "cube.npz"))
+    J_full = cli.primal(str(full), out=lambda s: None)
+    assert abs(J_full - c["value"]) < c["tolerance"]
+    pvd = ET.parse(tmp_path / f"out_{case}.pvd").getroot()
+    assert len(pvd.find("Collection")) == c["num_steps"]
+    vtu = ET.parse(tmp_path / f"out_{case}_0" / f"out_{case}_00.vtu").getroot()
+    piece = vtu.find("UnstructuredGrid").find("Piece")
+    assert int(piece.get("NumberOfCells")) == 132 and int(piece.get("NumberOfPoints")) == 51
+    names = {a.get("Name") for a in piece.iter("DataArray")}
+    assert {"u", "p", "sigma", "Fp", "eqps"} <= names
+
+    first = dict(c, num_steps=2, value=0.0, tolerance=1.0)
+    y1 = tmp_path / "first.yaml"
+    y1.write_text(_with_output(reference_style_yaml(case, first, "cube.npz").replace(
+        f"out file: out_{case}", "out file: out_first"), **{"write native": "true"}))
+    cli.primal(str(y1), out=lambda s: None)
+    assert (tmp_path / "out_first_1" / "restart.npz").exists()
+    second = dict(c, num_steps=1)
+    y2 = tmp_path / "second.yaml"
+    y2.write_text(reference_style_yaml(case, second, "out_first_1/").replace(
+        "initial time: 0.0", "initial time: 2.0").replace(f"out file: out_{case}", "out file: out_second"))
+    J_restart = cli.primal(str(y2), out=lambda s: None)
+    assert J_restart == J_full
+
+
+@pytest.mark.gpu
+def test_cli_nested_prints_estimate_and_size_field(tmp_path, monkeypatch):
+    import shutil
+    from goal_gb300 import cli
+    monkeypatch.chdir(tmp_path)
+    case = "J2_uniaxial_3D"
+    c = _cases()[case]
+    shutil.copy(os.path.join(ROOT, "tests", "golden", "cube_mesh.npz"), tmp_path / "cube.npz")
+    text = reference_style_yaml(case, c, "cube.npz").replace(
+        "  output:\n", "  adjoint mode: uniform\n  adaptation:\n    adapt cycles: 1\n    target elems: 500\n  output:\n")
+    y = tmp_path / "nested.yaml"
+    y.write_text(text)
+    lines = []
+    r = cli.nested(str(y), out=lines.append)
+    assert abs(r["J"] - c["value"]) < c["tolerance"]
+    assert sum(l.startswith(" > z.R = ") for l in lines) == c["num_steps"]
+    assert sum(l.startswith(" > |J(u)-J(uh)| < ") for l in lines) == c["num_steps"]
+    import numpy as np
+    assert np.all(np.isfinite(r["size"])) and r["size"].min() > 0
