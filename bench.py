@@ -332,6 +332,25 @@ def adjoint_leg(n, api):
     return out
 
 
+# ------------------------------------------------------------------ replicas
+def max_over_ranks(x: float, world: int, device: str) -> float:
+    """The slowest rank's time: every rank runs the same replica workload (no
+    collective on the data path) and the job takes as long as its slowest
+    replica."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(elements_per_replica: int, ms: float, world: int) -> float:
+    """Whole-job throughput: every replica's elements over the slowest replica's time."""
+    return world * elements_per_replica / (ms * 1e-3)
+
+
 # ------------------------------------------------------------------ GPU leg
 def main():
     a = _args()
@@ -395,11 +414,7 @@ def main():
     elem_ms = phase_ms[0] / max(1, phase_n.value)
     gather_ms = phase_ms[1] / max(1, phase_n.value)
     barrier()
-    ms = ev0.elapsed_time(ev1) / a.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / a.steps, world, "cuda")
 
     # end to end through the public API: pinned host U in, host R out, every step
     Uh = torch.from_numpy(U.ravel().copy()).pin_memory()
@@ -419,14 +434,14 @@ def main():
         L.goal_sol_info_get_vector(s.h, 0, ctypes.c_void_p(Rh.data_ptr()))
     e1.record(stream)
     e1.synchronize()
-    e2e_ms = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0)) / a.steps
+    e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0)) / a.steps, world, "cuda")
     barrier()
     clk = clocks.stop(local)
 
     if rank != 0:
         return 0
     E = mesh.num_elems
-    value = world * E / (ms * 1e-3)
+    value = replica_value(E, ms, world)
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
         with open(peaks_path) as f:
@@ -458,7 +473,7 @@ def main():
                    "elements": E, "nodes": mesh.num_nodes, "nnz": d.nnz, "colors": d.num_colors,
                    "yield_fraction": round(frac, 4), "l2": "working set > L2 (no flush)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": world * E / (e2e_ms * 1e-3), "unit": "elem/s", "h2d_bytes_per_step": 8 * 4 * mesh.num_nodes,
+        "e2e": {"value": replica_value(E, e2e_ms, world), "unit": "elem/s", "h2d_bytes_per_step": 8 * 4 * mesh.num_nodes,
                 "d2h_bytes_per_step": 8 * 4 * mesh.num_nodes},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
