@@ -47,6 +47,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--adjoint-n", type=int, default=40, help="base mesh of the adjoint-solve leg (0: skip)")
+    ap.add_argument("--learned-eval", type=int, default=20,
+                    help="held-out seeds of the learned-preconditioner study (0: skip)")
     return ap.parse_args()
 
 
@@ -332,6 +334,115 @@ def adjoint_leg(n, api):
     return out
 
 
+# ------------------------------------------------------------------ learned-preconditioner study
+BLOCK_REGIONS = 8
+
+
+def _block_problem(api, seed, target, steps):
+    """One seeded problem of the learned-preconditioner study: the 4x1x1 block
+    graded by three Gaussian bumps (h ratio 8) in 8 material regions with
+    E ~ lognormal(ln 1000, 0.5), nu ~ U[0.2, 0.45]; neo-Hookean for even seeds,
+    J2 (Y ~ U[50, 300], K = 100) for odd ones; u = 0 on x=0, u_x = 0.04 t on
+    x=4, ``steps`` load steps. Returns the converged problem and its systems:
+    the Newton Jacobian of every step and the adjoint (transposed) Jacobian of
+    the last, each with avg disp's dM/du."""
+    from goal_gb300.mesh import graded_block
+    rng = np.random.default_rng(1000 + seed)
+    mesh = graded_block(target, seed=seed, regions=BLOCK_REGIONS)
+    model = api.J2 if seed % 2 else api.NEOHOOKEAN
+    mats = [[float(rng.lognormal(np.log(1000.0), 0.5)), float(rng.uniform(0.2, 0.45)), 100.0,
+             float(rng.uniform(50.0, 300.0)), 1.0] for _ in range(BLOCK_REGIONS)]
+    d = api.Disc(mesh)
+    m = api.Mechanics(d, model, mats)
+    s = api.SolInfo(d)
+    bcs = api.Bcs(d, [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", "0.04*t")], [])
+    prm = api.solve_params(tolerance=1e-10, precision=api.MIXED, inner_iters=30, krylov_size=30, max_iters=3000)
+    systems = []
+    for k in range(1, steps + 1):
+        if k > 1:
+            m.update_states()
+        api.primal_solve(m, s, bcs, float(k), float(k - 1), 15, 1e-8, prm)
+        sk = api.SolInfo(d)
+        api.assemble(m, sk, api.PRIMAL, jacobian=True, save_states=False, qoi=api.QOI_AVG_DISP)
+        api.set_jac_dbcs(m, sk, bcs, float(k))
+        systems.append(("primal", sk))
+    sa = api.SolInfo(d)
+    api.assemble(m, sa, api.ADJOINT, jacobian=True, save_states=False, qoi=api.QOI_AVG_DISP)
+    api.set_jac_dbcs(m, sa, bcs, float(steps))
+    systems.append(("adjoint", sa))
+    return (mesh, d, m, s, bcs), systems
+
+
+def learned_eval_leg(api, held_out, train_problems=8, train_target=20000, eval_target=50000):
+    """Train the network on the systems of ``train_problems`` seeded block
+    problems (5 load steps each: every Newton Jacobian plus the adjoint one),
+    then solve the last Newton Jacobian and the adjoint system of ``held_out``
+    other seeds (3 load steps), right-hand side avg disp's dM/du, to 1e-10
+    with FP32-inner / FP64-outer FGMRES, once with plain block-Jacobi and once
+    with the network: outer iterations, seconds and how often the cap (750
+    outer iterations) sent the solve back to plain block-Jacobi. (Plain FP64
+    block-Jacobi FGMRES(100) needs more than 20,000 iterations on most of
+    these graded, heterogeneous systems.)"""
+    t0 = time.perf_counter()
+    keep, train = [], []
+    failed = 0
+    for seed in range(train_problems):
+        try:
+            prob, systems = _block_problem(api, seed, train_target, 5)
+        except api.GoalError:
+            failed += 1
+            continue
+        keep.append(prob)
+        train += [sk for _, sk in systems]
+        keep.append(systems)
+    net = api.Learned(seed=0)
+    t1 = time.perf_counter()
+    losses = net.train(train, epochs=40, lr=2e-3, num_probes=8)
+    t_train = time.perf_counter() - t1
+    out = {"train": {"problems": train_problems - failed, "systems": len(train), "elements_each": train_target,
+                     "seconds_generate": t1 - t0, "seconds_train": t_train, "loss_first": float(losses[0]),
+                     "loss_last": float(losses[-1]), "newton_failures": failed},
+           "held_out": held_out, "elements_each": eval_target, "tolerance": 1e-10}
+    rows = {k: [] for k in ("primal", "adjoint")}
+    eval_failed = 0
+    mix = dict(krylov_size=30, tolerance=1e-10, max_iters=1500, precision=api.MIXED, inner_iters=30)
+    for seed in range(100, 100 + held_out):
+        try:
+            (mesh, d, m, s, bcs), systems = _block_problem(api, seed, eval_target, 3)
+        except api.GoalError:
+            eval_failed += 1
+            continue
+        for kind, sk in (systems[-2], systems[-1]):
+            b = sk.dMdu
+            _, plain = api.solve(sk, b, params=api.solve_params(**mix))
+            net.attach(sk)
+            _, lrn = api.solve(sk, b, params=api.solve_params(precond=api.PRECOND_LEARNED, learned_cap=750, **mix))
+            rows[kind].append((plain, lrn))
+    out["newton_failures"] = eval_failed
+
+    def summary(rs):
+        if not rs:
+            return None
+
+        def med(f):
+            return float(statistics.median(f(r) for r in rs))
+        return {"cases": len(rs),
+                "outer_iters_plain_median": med(lambda r: r[0]["iters"]),
+                "outer_iters_learned_median": med(lambda r: r[1]["iters"]),
+                "seconds_plain_median": med(lambda r: r[0]["seconds"]),
+                "seconds_learned_median": med(lambda r: r[1]["seconds"]),
+                "time_ratio_median": med(lambda r: r[0]["seconds"] / max(1e-9, r[1]["seconds"])),
+                "time_ratio_min": float(min(r[0]["seconds"] / max(1e-9, r[1]["seconds"]) for r in rs)),
+                "learned_slower": sum(1 for r in rs if r[1]["seconds"] > r[0]["seconds"]),
+                "fallback_rate": sum(1 for r in rs if r[1]["fell_back"]) / float(len(rs)),
+                "converged_plain": sum(1 for r in rs if r[0]["converged"]),
+                "converged_learned": sum(1 for r in rs if r[1]["converged"])}
+    out["newton_jacobian"] = summary(rows["primal"])
+    out["adjoint"] = summary(rows["adjoint"])
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 # ------------------------------------------------------------------ replicas
 def max_over_ranks(x: float, world: int, device: str) -> float:
     """The slowest rank's time: every rank runs the same replica workload (no
@@ -484,6 +595,11 @@ def main():
                      "binding_roof": "fp64", "fp64": fp64},
         "clocks": clk,
     }
+    if a.learned_eval > 0:
+        try:
+            line["learned_eval"] = learned_eval_leg(api, a.learned_eval)
+        except Exception as exc:
+            line["learned_eval"] = {"error": str(exc)[:300]}
     if a.adjoint_n > 0:
         try:
             line["adjoint_solve"] = adjoint_leg(a.adjoint_n, api)

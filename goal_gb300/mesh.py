@@ -128,12 +128,15 @@ def kuhn_cube(n: int, length=(1.0, 1.0, 1.0), set_name: str = "cube", jitter: fl
                 node_sets=node_sets, side_sets=side_sets)
 
 
-def graded_block(target_elems: int, seed: int = 0, h_ratio: float = 8.0, set_name: str = "block") -> Mesh:
+def graded_block(target_elems: int, seed: int = 0, h_ratio: float = 8.0, set_name: str = "block",
+                 regions: int = 1) -> Mesh:
     """4x1x1 block meshed with Kuhn tets on a tensor grid graded by a smooth
     seeded size field made of three Gaussian bumps (h ratio up to ``h_ratio``).
 
     The grading is separable (one 1-D spacing per axis, each the marginal of
     the 3-D size field), so the mesh stays a conforming Kuhn triangulation.
+    regions > 1 splits the block into that many element sets ("region<i>"),
+    the Voronoi cells of seeded points, for piecewise-constant materials.
     """
     rng = np.random.default_rng(seed)
     centers = rng.uniform([0.0, 0.0, 0.0], [4.0, 1.0, 1.0], size=(3, 3))
@@ -181,8 +184,15 @@ def graded_block(target_elems: int, seed: int = 0, h_ratio: float = 8.0, set_nam
     tets = np.stack(tets, axis=1).reshape(-1, 4).astype(np.int32)
     tets = orient_positive(coords, tets)
     node_sets, side_sets = _plane_sets(coords, tets, np.zeros(3), lengths, 1e-12)
-    return Mesh(coords=np.ascontiguousarray(coords), tets=tets,
-                elem_set=np.zeros(tets.shape[0], np.int32), elem_set_names=[set_name],
+    elem_set = np.zeros(tets.shape[0], np.int32)
+    names = [set_name]
+    if regions > 1:
+        pts = rng.uniform([0.0, 0.0, 0.0], lengths, size=(regions, 3))
+        cent = coords[tets].mean(axis=1)
+        d2 = ((cent[:, None, :] - pts[None, :, :]) ** 2).sum(axis=2)
+        elem_set = np.argmin(d2, axis=1).astype(np.int32)
+        names = [f"region{i}" for i in range(regions)]
+    return Mesh(coords=np.ascontiguousarray(coords), tets=tets, elem_set=elem_set, elem_set_names=names,
                 node_sets=node_sets, side_sets=side_sets)
 
 
