@@ -27,6 +27,11 @@ struct GState {
 
 constexpr int kMaxM = 256;
 constexpr int kDotChunk = 8;
+// Gram-Schmidt passes: the FP64 outer basis gets the conditional second pass;
+// the fixed-length FP32 inner solve is only a preconditioner of the flexible
+// outer solve and takes one pass (measured on the nested adjoints: same outer
+// iteration counts, 25% less inner time).
+constexpr int kOuterPasses = 2, kInnerPasses = 1;
 constexpr int kMaxRows = 8;  // rows per thread in the orthogonalization kernels: 1, 2, 4 or 8
 
 template <typename T>
@@ -616,11 +621,11 @@ namespace {
 // first one removed more than half of |w|^2 (device-side decision).
 template <typename T, int R>
 void orth_passes(long long n, T* V, T* w, GState* st, double* H, int ldh, double* dots, double* red, int jmax,
-                 cudaStream_t s) {
+                 int passes, cudaStream_t s) {
   const int nbx = slab_grid(n, R);
   double* part = red;
   double* npart = red + (size_t)(kMaxM + 2) * nbx;
-  for (int pass = 0; pass < 2; ++pass) {
+  for (int pass = 0; pass < passes; ++pass) {
     k_multidot<T, R><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
     GOAL_CHECK_LAUNCH();
     k_dots_fin<<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
@@ -636,12 +641,12 @@ void orth_passes(long long n, T* V, T* w, GState* st, double* H, int ldh, double
 // normalization and Givens update, on state st.
 template <typename T>
 void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, double* cs, double* sn, double* g,
-                  double* dots, double* red, int jmax, double tol_abs, cudaStream_t s) {
+                  double* dots, double* red, int jmax, double tol_abs, int passes, cudaStream_t s) {
   switch (slab_rows<T>(n)) {
-    case 1: orth_passes<T, 1>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
-    case 2: orth_passes<T, 2>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
-    case 4: orth_passes<T, 4>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
-    default: orth_passes<T, 8>(n, V, w, st, H, ldh, dots, red, jmax, s); break;
+    case 1: orth_passes<T, 1>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
+    case 2: orth_passes<T, 2>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
+    case 4: orth_passes<T, 4>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
+    default: orth_passes<T, 8>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
   }
   k_normalize<T><<<vec_grid(n), 256, 0, s>>>(n, V, n, w, st, H, ldh);
   GOAL_CHECK_LAUNCH();
@@ -773,7 +778,8 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
         k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
                                                        K.w32.ptr);
         GOAL_CHECK_LAUNCH();
-        arnoldi_orth<float>(n, K.V32.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0, s);
+        arnoldi_orth<float>(n, K.V32.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0,
+                            kInnerPasses, s);
       }
       k_backsolve<<<1, 1, 0, s>>>(sti, Hin, mi + 1, gin, yin);
       GOAL_CHECK_LAUNCH();
@@ -795,7 +801,7 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
     k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
     GOAL_CHECK_LAUNCH();
     arnoldi_orth<double>(n, K.V.ptr, K.w.ptr, st, K.H.ptr, m + 1, K.cs.ptr, K.sn.ptr, K.g.ptr, dots, K.red.ptr, m,
-                         tol_abs, s);
+                         tol_abs, kOuterPasses, s);
   };
   // one Arnoldi step as a CUDA graph, captured once per solve; its kernels are
   // gated on the device state, so steps launched past the end of a cycle are
