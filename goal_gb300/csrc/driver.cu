@@ -141,7 +141,7 @@ BsrView bsr_view(const Disc& d) {
 SolveStats linear_solve(SolInfo& s, const SolveParams& p, const double* b, double* x, Krylov& K, const double* dD) {
   K.stream = s.disc->stream;
   BsrView A = bsr_view(*s.disc);
-  if (p.precision == PREC_MIXED) make_fp32_copy(A, s.A.ptr, K);
+  if (p.precision == PREC_MIXED) make_inner_copy(A, s.A.ptr, K);
   if (p.precond == PRECOND_LEARNED) {
     GOAL_REQUIRE(s.learned, GOAL_ERR_STATE, "learned preconditioner requested but no network is attached");
     s.learned->stream = K.stream;

@@ -9,6 +9,8 @@
 
 #include "krylov.cuh"
 
+#include <cuda_fp16.h>
+
 #include <type_traits>
 
 namespace goal {
@@ -51,18 +53,32 @@ struct Vec4<float> {
   }
 };
 
+// One row of a 4x4 matrix block in the arithmetic type T: same-type loads, or
+// four binary16 values (the inner solve's matrix) widened to float.
+template <typename T, typename TA>
+__device__ __forceinline__ void load_row(const TA* p, T& a, T& b, T& c, T& d) {
+  Vec4<T>::load(p, a, b, c, d);
+}
+template <>
+__device__ __forceinline__ void load_row<float, __half>(const __half* p, float& a, float& b, float& c, float& d) {
+  const uint2 u = *reinterpret_cast<const uint2*>(p);
+  const float2 f0 = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+  const float2 f1 = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+  a = f0.x; b = f0.y; c = f1.x; d = f1.y;
+}
+
 // Block-row product of node n, row r: sum_k A_k[r,:] . x_{bcol[k]}, one fused
 // multiply-add per matrix entry (on GB300 the FP64 pipe, not HBM, bounds the
 // FP64 kernels, so no operation is spent on reductions).
-template <typename T>
-__device__ __forceinline__ T block_row_dot(const int* __restrict__ bcol, const T* __restrict__ A,
+template <typename T, typename TA>
+__device__ __forceinline__ T block_row_dot(const int* __restrict__ bcol, const TA* __restrict__ A,
                                            const T* __restrict__ x, int b0, int b1, int r) {
   T acc = T(0);
 #pragma unroll 4
   for (int k = b0; k < b1; ++k) {
     const int c = __ldg(bcol + k);
     T a0, a1, a2, a3, x0, x1, x2, x3;
-    Vec4<T>::load(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+    load_row<T, TA>(A + 16ll * k + 4 * r, a0, a1, a2, a3);
     Vec4<T>::load(x + 4ll * c, x0, x1, x2, x3);
     acc = fma(a0, x0, acc);
     acc = fma(a1, x1, acc);
@@ -74,14 +90,14 @@ __device__ __forceinline__ T block_row_dot(const int* __restrict__ bcol, const T
 
 // y = A x  (or y = b - A x). Four threads per block row (one per row of the
 // node's 4x4 blocks), no cross-thread reduction.
-template <typename T, bool RESID>
+template <typename T, typename TA, bool RESID>
 __global__ void __launch_bounds__(256) k_spmv(int N, const int* __restrict__ brow_ptr, const int* __restrict__ bcol,
-                                              const T* __restrict__ A, const T* __restrict__ x,
+                                              const TA* __restrict__ A, const T* __restrict__ x,
                                               const T* __restrict__ b, T* __restrict__ y) {
   const int r = threadIdx.x & 3;
   const int nq = (gridDim.x * blockDim.x) >> 2;
   for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; n < N; n += nq) {
-    const T acc = block_row_dot(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
+    const T acc = block_row_dot<T, TA>(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
     if (RESID) y[4ll * n + r] = b[4ll * n + r] - acc;
     else y[4ll * n + r] = acc;
   }
@@ -150,16 +166,16 @@ __global__ void k_second_sweep_col(int N, const T* __restrict__ B, const T* V, l
 }
 
 // w = A z_j with z_j = column j of Z
-template <typename T>
+template <typename T, typename TA>
 __global__ void __launch_bounds__(256) k_spmv_col(int N, const int* __restrict__ brow_ptr,
-                                                  const int* __restrict__ bcol, const T* __restrict__ A,
+                                                  const int* __restrict__ bcol, const TA* __restrict__ A,
                                                   const T* Z, long long ld, const GState* st, T* __restrict__ y) {
   if (st->done) return;
   const T* x = Z + (long long)st->j * ld;
   const int r = threadIdx.x & 3;
   const int nq = (gridDim.x * blockDim.x) >> 2;
   for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; n < N; n += nq)
-    y[4ll * n + r] = block_row_dot(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
+    y[4ll * n + r] = block_row_dot<T, TA>(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
 }
 
 // Orthogonalization kernels work on row slabs of 256 x R rows per block:
@@ -446,25 +462,27 @@ __global__ void k_scale_into(long long n, const TR* r, const GState* st, T* v0) 
     v0[i] = (T)r[i] * inv;
 }
 
-__global__ void k_col_to_f32(long long n, const double* V, long long ld, const GState* st, float* out) {
+// The inner solve works in the dof-scaled space: r^ = S r in, z = S z^ out.
+__global__ void k_col_to_f32(long long n, const double* V, long long ld, const GState* st, const double* sd,
+                             float* out) {
   if (st->done) return;
   const double* v = V + (long long)st->j * ld;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    out[i] = (float)v[i];
+    out[i] = (float)(v[i] * sd[i]);
 }
-__global__ void k_f32_to_col(long long n, const float* in, double* Z, long long ld, const GState* st) {
+__global__ void k_f32_to_col(long long n, const float* in, const double* sd, double* Z, long long ld,
+                             const GState* st) {
   if (st->done) return;
   double* z = Z + (long long)st->j * ld;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    z[i] = (double)in[i];
+    z[i] = (double)in[i] * sd[i];
 }
 // inner solve runs only when the outer step is live
 __global__ void k_gate(const GState* outer, GState* inner) {
   if (outer->done) inner->done = 1;
 }
 
-__global__ void k_bj_setup(int N, const int* diag, const double* A, const double* dD, double* Dinv, float* Dinv32,
-                           int* singular) {
+__global__ void k_bj_setup(int N, const int* diag, const double* A, const double* dD, double* Dinv, int* singular) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
     double a[4][8];
     const double* blk = A + 16ll * diag[n];
@@ -497,9 +515,7 @@ __global__ void k_bj_setup(int N, const int* diag, const double* A, const double
     if (!ok) atomicAdd(singular, 1);
     for (int r = 0; r < 4; ++r)
       for (int c = 0; c < 4; ++c) {
-        double v = ok ? a[r][4 + c] : (r == c ? 1.0 : 0.0);
-        Dinv[16ll * n + 4 * r + c] = v;
-        if (Dinv32) Dinv32[16ll * n + 4 * r + c] = (float)v;
+        Dinv[16ll * n + 4 * r + c] = ok ? a[r][4 + c] : (r == c ? 1.0 : 0.0);
       }
   }
 }
@@ -526,9 +542,39 @@ __global__ void k_lift_identity_rows(int N, const int* brow_ptr, const int* bcol
   }
 }
 
-__global__ void k_to_f32(long long n, const double* in, float* out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    out[i] = (float)in[i];
+// dof scales S = diag(|a_ii|^-1/2) (1 for a zero diagonal)
+__global__ void k_dof_scale(int N, const int* __restrict__ diag, const double* __restrict__ A, double* sd) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
+    const double d = fabs(A[16ll * diag[i >> 2] + 5 * (i & 3)]);
+    sd[i] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+  }
+}
+// A^ = S A S in binary16 (saturated to the finite range); thread = (node, row)
+__global__ void k_to_half_scaled(int N, const int* __restrict__ brow_ptr, const int* __restrict__ bcol,
+                                 const double* __restrict__ A, const double* __restrict__ sd, __half* A16) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 4 * N; t += gridDim.x * blockDim.x) {
+    const int n = t >> 2, r = t & 3;
+    const double sr = sd[t];
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      const int m = bcol[k];
+      for (int c = 0; c < 4; ++c) {
+        double v = sr * A[16ll * k + 4 * r + c] * sd[4ll * m + c];
+        v = fmin(fmax(v, -65504.0), 65504.0);
+        A16[16ll * k + 4 * r + c] = __double2half(v);
+      }
+    }
+  }
+}
+// the preconditioner blocks in the scaled space: D^-1 -> S^-1 D^-1 S^-1 and
+// (learned second sweep) B -> S^-1 B S^-1, in FP32
+__global__ void k_inner_blocks(int N, const double* __restrict__ Dinv, const double* __restrict__ Bc,
+                               const double* __restrict__ sd, float* Dinv32, float* Bc32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) {
+    const int n = i >> 4, r = (i >> 2) & 3, c = i & 3;
+    const double s = sd[4ll * n + r] * sd[4ll * n + c];
+    Dinv32[i] = (float)(Dinv[i] / s);
+    if (Bc) Bc32[i] = (float)(Bc[i] / s);
+  }
 }
 
 int spmv_grid(int N) { return grid_for((long long)N * 4, 256, kSMs * 16); }
@@ -578,7 +624,7 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
     need(sni, mi_ + 1);
     need(gi, mi_ + 2);
     need(yi, mi_ + 1);
-    need(A32, 16ull * nnzb);
+
   }
   n = n_;
   m = m_;
@@ -588,11 +634,10 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
 int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, Krylov& K) {
   const int N = A.num_nodes;
   need(K.Dinv, 16ull * N);
-  need(K.Dinv32, 16ull * N);
   need(K.flag, 8);
   K.two_sweep = false;
   GOAL_CUDA(cudaMemsetAsync(K.flag.ptr, 0, sizeof(int), K.stream));
-  k_bj_setup<<<grid_for(N, 128), 128, 0, K.stream>>>(N, A.diag, vals, dD, K.Dinv.ptr, K.Dinv32.ptr, K.flag.ptr);
+  k_bj_setup<<<grid_for(N, 128), 128, 0, K.stream>>>(N, A.diag, vals, dD, K.Dinv.ptr, K.flag.ptr);
   GOAL_CHECK_LAUNCH();
   int sing = 0;
   GOAL_CUDA(cudaMemcpyAsync(&sing, K.flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, K.stream));
@@ -600,18 +645,19 @@ int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, K
   return sing;
 }
 
-void make_fp32_copy(const BsrView& A, const double* vals, Krylov& K) {
-  need(K.A32, 16ull * A.nnzb);
-  k_to_f32<<<vec_grid(16ll * A.nnzb), 256, 0, K.stream>>>(16ll * A.nnzb, vals, K.A32.ptr);
+void make_inner_copy(const BsrView& A, const double* vals, Krylov& K) {
+  const int N = A.num_nodes;
+  need(K.sd, 4ull * N);
+  need(K.A16, 16ull * A.nnzb);
+  k_dof_scale<<<grid_for(4ll * N, 256), 256, 0, K.stream>>>(N, A.diag, vals, K.sd.ptr);
+  GOAL_CHECK_LAUNCH();
+  k_to_half_scaled<<<grid_for(4ll * N, 256), 256, 0, K.stream>>>(N, A.brow_ptr, A.bcol, vals, K.sd.ptr, K.A16.ptr);
   GOAL_CHECK_LAUNCH();
 }
 
 void spmv64(const BsrView& A, const double* vals, const double* x, double* y, cudaStream_t s) {
-  k_spmv<double, false><<<spmv_grid(A.num_nodes), 256, 0, s>>>(A.num_nodes, A.brow_ptr, A.bcol, vals, x, nullptr, y);
-  GOAL_CHECK_LAUNCH();
-}
-void spmv32(const BsrView& A, const float* vals, const float* x, float* y, cudaStream_t s) {
-  k_spmv<float, false><<<spmv_grid(A.num_nodes), 256, 0, s>>>(A.num_nodes, A.brow_ptr, A.bcol, vals, x, nullptr, y);
+  k_spmv<double, double, false><<<spmv_grid(A.num_nodes), 256, 0, s>>>(A.num_nodes, A.brow_ptr, A.bcol, vals, x, nullptr,
+                                                                      y);
   GOAL_CHECK_LAUNCH();
 }
 
@@ -714,7 +760,14 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
   K.reserve((int)n, m, mi, mixed, A.nnzb);
   cudaStream_t s = K.stream;
   GOAL_REQUIRE(K.Dinv.ptr, GOAL_ERR_STATE, "fgmres: block-Jacobi preconditioner not set up");
-  if (mixed) GOAL_REQUIRE(K.A32.ptr, GOAL_ERR_STATE, "fgmres: FP32 matrix copy missing");
+  if (mixed) {
+    GOAL_REQUIRE(K.A16.ptr && K.sd.ptr, GOAL_ERR_STATE, "fgmres: inner matrix copy missing");
+    need(K.Dinv32, 16ull * N);
+    if (K.two_sweep) need(K.Bc32, 16ull * N);
+    k_inner_blocks<<<grid_for(16ll * N, 256), 256, 0, s>>>(N, K.Dinv.ptr, K.two_sweep ? K.Bc.ptr : nullptr, K.sd.ptr,
+                                                          K.Dinv32.ptr, K.Bc32.ptr);
+    GOAL_CHECK_LAUNCH();
+  }
 
   GState* st = reinterpret_cast<GState*>(K.scal.ptr);         // outer state
   GState* sti = reinterpret_cast<GState*>(K.scal.ptr + 24);   // inner state
@@ -730,7 +783,7 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
   k_lift_identity_rows<<<grid_for(n, 256), 256, 0, s>>>(N, A.brow_ptr, A.bcol, A.diag, vals, b, x);
   GOAL_CHECK_LAUNCH();
   // r = b - A x
-  k_spmv<double, true><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, x, b, K.r.ptr);
+  k_spmv<double, double, true><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, x, b, K.r.ptr);
   GOAL_CHECK_LAUNCH();
   out.spmv64++;
   double beta = read_norm(n, K.r.ptr, K);
@@ -745,15 +798,16 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       k_bj_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv.ptr, K.V.ptr, K.Z.ptr, n, st);
       GOAL_CHECK_LAUNCH();
       if (sweep2) {
-        k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
+        k_spmv_col<double, double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
         GOAL_CHECK_LAUNCH();
         k_second_sweep_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc.ptr, K.V.ptr, n, K.w.ptr, K.Z.ptr, n, st);
         GOAL_CHECK_LAUNCH();
       }
     } else {
-      // inner FP32 GMRES on A32 with the right preconditioner, fixed mi
-      // iterations: Z_j = M^-1 V32 y with V32 the inner basis started from V_j
-      k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.r32.ptr);
+      // inner GMRES in the dof-scaled space (FP32 vectors, A^ = S A S in
+      // binary16) with the right preconditioner, fixed mi iterations:
+      // Z_j = S M^-1 V32 y with V32 the inner basis started from S V_j
+      k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.sd.ptr, K.r32.ptr);
       GOAL_CHECK_LAUNCH();
       k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.red.ptr);
       GOAL_CHECK_LAUNCH();
@@ -764,18 +818,18 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       k_scale_into<float, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V32.ptr);
       GOAL_CHECK_LAUNCH();
       for (int it = 0; it < mi; ++it) {
-        // r32 = M^-1 v_it ; w32 = A32 r32 (ld 0 keeps the input at r32)
+        // r32 = M^-1 v_it ; w32 = A^ r32 (ld 0 keeps the input at r32)
         k_bj_colin<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V32.ptr, n, sti, K.r32.ptr);
         GOAL_CHECK_LAUNCH();
         if (sweep2) {
-          k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
+          k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
                                                          K.t32.ptr);
           GOAL_CHECK_LAUNCH();
           k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V32.ptr, n, K.t32.ptr,
                                                                      K.r32.ptr, 0, sti);
           GOAL_CHECK_LAUNCH();
         }
-        k_spmv_col<float><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, 0, sti,
+        k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
                                                        K.w32.ptr);
         GOAL_CHECK_LAUNCH();
         arnoldi_orth<float>(n, K.V32.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0,
@@ -788,17 +842,17 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       k_bj<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.w32.ptr, K.r32.ptr);
       GOAL_CHECK_LAUNCH();
       if (sweep2) {
-        k_spmv<float, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A32.ptr, K.r32.ptr, nullptr,
-                                                          K.t32.ptr);
+        k_spmv<float, __half, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, nullptr,
+                                                                   K.t32.ptr);
         GOAL_CHECK_LAUNCH();
         k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.w32.ptr, 0, K.t32.ptr,
                                                                    K.r32.ptr, 0, nullptr);
         GOAL_CHECK_LAUNCH();
       }
-      k_f32_to_col<<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.Z.ptr, n, st);
+      k_f32_to_col<<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.sd.ptr, K.Z.ptr, n, st);
       GOAL_CHECK_LAUNCH();
     }
-    k_spmv_col<double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
+    k_spmv_col<double, double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
     GOAL_CHECK_LAUNCH();
     arnoldi_orth<double>(n, K.V.ptr, K.w.ptr, st, K.H.ptr, m + 1, K.cs.ptr, K.sn.ptr, K.g.ptr, dots, K.red.ptr, m,
                          tol_abs, kOuterPasses, s);
@@ -843,7 +897,7 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
     GOAL_CHECK_LAUNCH();
     k_combine<double, double><<<nbx, 256, 0, s>>>(n, K.Z.ptr, n, K.y.ptr, st, x, 0);
     GOAL_CHECK_LAUNCH();
-    k_spmv<double, true><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, x, b, K.r.ptr);
+    k_spmv<double, double, true><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, x, b, K.r.ptr);
     GOAL_CHECK_LAUNCH();
     out.spmv64++;
     double nb = read_norm(n, K.r.ptr, K);

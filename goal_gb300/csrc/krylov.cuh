@@ -15,6 +15,8 @@
 // estimate per outer iteration.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 
 namespace goal {
@@ -56,7 +58,10 @@ struct Krylov {
   int n = 0, m = 0, mi = 0;
   DevBuf<double> V, Z, w, r, H, cs, sn, g, y, red, scal, dots;
   DevBuf<double> Hi, csi, sni, gi, yi;   // inner (FP32 solve) Hessenberg and rotations
-  DevBuf<float> V32, w32, r32, t32, A32;
+  DevBuf<float> V32, w32, r32, t32;
+  // mixed mode: the inner solve's matrix S A S in binary16, S = diag(|a_ii|^-1/2)
+  DevBuf<__half> A16;
+  DevBuf<double> sd;
   DevBuf<double> Dinv;       // 16 x N inverse diagonal blocks (FP64)
   DevBuf<float> Dinv32;
   // learned two-sweep form: P r = z + B (r - A z), z = D^-1 r (B: 16 x N)
@@ -73,11 +78,10 @@ struct Krylov {
 // 16 x N, added before inversion) and selects plain block-Jacobi. Returns the
 // number of singular blocks.
 int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, Krylov& K);
-// FP32 copy of the matrix values for the mixed solve.
-void make_fp32_copy(const BsrView& A, const double* vals, Krylov& K);
+// The mixed solve's inner matrix: dof scales S and S A S in binary16.
+void make_inner_copy(const BsrView& A, const double* vals, Krylov& K);
 
 void spmv64(const BsrView& A, const double* vals, const double* x, double* y, cudaStream_t s);
-void spmv32(const BsrView& A, const float* vals, const float* x, float* y, cudaStream_t s);
 
 // Solves A x = b (x holds the initial guess). All pointers are device pointers.
 SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double* x, const SolveParams& p, Krylov& K);

@@ -508,7 +508,7 @@ __global__ void k_adam(int n, float* p, const float* g, float* m1, float* m2, fl
 
 // B_n = S_n W_n S_n^-1 D_n^-1 (W = C with Dirichlet rows/columns zeroed)
 __global__ void k_write_B(int N, const double* Dinv, const float* C, const double* sd, const int* dmask,
-                          double* out64, float* out32) {
+                          double* out64) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) {
     int n = i >> 4, r = (i >> 2) & 3, c = i & 3;
     double acc = 0.0;
@@ -516,9 +516,7 @@ __global__ void k_write_B(int N, const double* Dinv, const float* C, const doubl
       for (int k = 0; k < 4; ++k)
         if (kept(dmask, n, k))
           acc += (double)C[16ll * n + 4 * r + k] / sd[4ll * n + k] * Dinv[16ll * n + 4 * k + c];
-    const double v = sd[4ll * n + r] * acc;
-    out64[i] = v;
-    out32[i] = (float)v;
+    out64[i] = sd[4ll * n + r] * acc;
   }
 }
 
@@ -737,9 +735,8 @@ void mpnn_apply_to_block_jacobi(Mpnn& net, const BsrMatrix& A, Krylov& K) {
   const int N = A.v.num_nodes;
   mpnn_forward(net, A, false);
   need(K.Bc, 16ull * N);
-  need(K.Bc32, 16ull * N);
   k_write_B<<<grid_for(16ll * N, 256), 256, 0, net.stream>>>(N, net.Dinv.ptr, net.C.ptr, net.sd.ptr, net.dmask.ptr,
-                                                             K.Bc.ptr, K.Bc32.ptr);
+                                                             K.Bc.ptr);
   GOAL_CHECK_LAUNCH();
   K.two_sweep = true;
 }

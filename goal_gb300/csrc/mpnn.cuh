@@ -75,7 +75,7 @@ void mpnn_forward(Mpnn& net, const BsrMatrix& A, bool keep);
 double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const double* probes_dev, unsigned seed);
 // Adam step on net.params with net.grad.
 void mpnn_adam(Mpnn& net, float lr, float beta1, float beta2, float eps);
-// Writes the second-sweep blocks B (FP64 and FP32) into the Krylov workspace
+// Writes the second-sweep blocks B (FP64) into the Krylov workspace
 // and switches its preconditioner to the two-sweep form; the plain D^-1
 // blocks must already be set up (block_jacobi_setup).
 void mpnn_apply_to_block_jacobi(Mpnn& net, const BsrMatrix& A, Krylov& K);
