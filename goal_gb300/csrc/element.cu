@@ -643,9 +643,26 @@ void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t 
   }
 }
 
+// Row r of contribution v (element slot v >> 4, element block v & 15) of the
+// element buffer; TRANSPOSE reads column r of the transposed element block.
+template <bool TRANSPOSE>
+__device__ __forceinline__ void load_contrib(const double* __restrict__ ebuf, int estride, int v, int r, double& x0,
+                                             double& x1, double& x2, double& x3) {
+  const int s = v >> 4, lb = v & 15;
+  if (TRANSPOSE) {
+    const int lt = ((lb & 3) << 2) | (lb >> 2);
+    const double* p = ebuf + (size_t)s * estride + 16 + 16 * lt + r;
+    x0 = __ldg(p); x1 = __ldg(p + 4); x2 = __ldg(p + 8); x3 = __ldg(p + 12);
+  } else {
+    ld4(ebuf + (size_t)s * estride + 16 + 16 * lb + 4 * r, x0, x1, x2, x3);
+  }
+}
+
 // Phase 2 of the two-phase assembly: every matrix block sums its element
 // blocks in element order (4 threads per block, one per row); TRANSPOSE
 // accumulates the element blocks transposed (ADJOINT mode stores dR/du^T).
+// Contributions are fetched four at a time (independent loads in flight),
+// then added in element order.
 template <bool TRANSPOSE>
 __global__ void __launch_bounds__(256) k_gather_blocks(int nnzb, const int* __restrict__ bptr,
                                                        const int* __restrict__ blist, const double* __restrict__ ebuf,
@@ -656,18 +673,21 @@ __global__ void __launch_bounds__(256) k_gather_blocks(int nnzb, const int* __re
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     if (accumulate) ld4(A + 16ll * k + 4 * r, a0, a1, a2, a3);
     const int c1 = __ldg(bptr + k + 1);
-    for (int c = __ldg(bptr + k); c < c1; ++c) {
-      const int v = __ldg(blist + c);
-      const int s = v >> 4, lb = v & 15;
-      if (TRANSPOSE) {
-        const int lt = ((lb & 3) << 2) | (lb >> 2);
-        const double* p = ebuf + (size_t)s * estride + 16 + 16 * lt + r;
-        a0 += __ldg(p); a1 += __ldg(p + 4); a2 += __ldg(p + 8); a3 += __ldg(p + 12);
-      } else {
-        double x0, x1, x2, x3;
-        ld4(ebuf + (size_t)s * estride + 16 + 16 * lb + 4 * r, x0, x1, x2, x3);
-        a0 += x0; a1 += x1; a2 += x2; a3 += x3;
+    int c = __ldg(bptr + k);
+    for (; c + 4 <= c1; c += 4) {
+      double x[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        load_contrib<TRANSPOSE>(ebuf, estride, __ldg(blist + c + q), r, x[q][0], x[q][1], x[q][2], x[q][3]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a0 += x[q][0]; a1 += x[q][1]; a2 += x[q][2]; a3 += x[q][3];
       }
+    }
+    for (; c < c1; ++c) {
+      double x0, x1, x2, x3;
+      load_contrib<TRANSPOSE>(ebuf, estride, __ldg(blist + c), r, x0, x1, x2, x3);
+      a0 += x0; a1 += x1; a2 += x2; a3 += x3;
     }
     st4(A + 16ll * k + 4 * r, a0, a1, a2, a3);
   }
