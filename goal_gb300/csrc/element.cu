@@ -426,6 +426,10 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
     vq = fmu * (2.0 * alpha / 3.0);
   }
   double Xp[4][3], Yp[4][3], nv[4][3];
+  // X_b = V(-2/3 ga m_b + pJ h_b), Y_b = V(-2/3 ga h_b + alpha (yq q_b + yh h_b + yn n_b)),
+  // with the coefficients folded once per element
+  const double xm = V * (-(2.0 / 3.0) * ga), xh = V * pJ;
+  const double yhc = V * (-(2.0 / 3.0) * ga + alpha * yh), yqc = V * (alpha * yq), ync = V * (alpha * yn);
 #pragma unroll
   for (int b = 0; b < 4; ++b) {
     if (need_n) {
@@ -437,8 +441,8 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      Xp[b][k] = V * (-(2.0 / 3.0) * ga * mv[b][k] + pJ * hv[b][k]);
-      Yp[b][k] = V * (-(2.0 / 3.0) * ga * hv[b][k] + alpha * (yq * qv[b][k] + yh * hv[b][k] + yn * nv[b][k]));
+      Xp[b][k] = fma(xm, mv[b][k], xh * hv[b][k]);
+      Yp[b][k] = need_n ? fma(yhc, hv[b][k], fma(yqc, qv[b][k], ync * nv[b][k])) : yhc * hv[b][k];
     }
   }
   // dM/du (QoI derivative) for the u dofs; pressure dofs do not enter the QoIs
@@ -467,23 +471,30 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   const double tJV = tauJ * V;
   const double ppc = V * pp_coef;
   const double pu0 = V * ((J + Jinv) * 0.125);
+  // stabilization coefficients of the p-u rows, folded once per element
+  double tvv[3], twv[4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) tvv[k] = a.stab ? tJV * vv[k] : 0.0;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) twv[b] = a.stab ? tJV * wv[b] : 0.0;
+  const double tJVs = a.stab ? tJV : 0.0;
   const unsigned fm = (!BUF && a.overwrite) ? __ldg(a.d.first + s) : 0u;
 #pragma unroll
   for (int ai = 0; ai < 4; ++ai) {
-    double CG[3];  // C G_a
+    double CG[3];  // ga V C G_a
     if constexpr (MODEL == MODEL_J2) {
-      CG[0] = C[0] * G[ai][0] + C[3] * G[ai][1] + C[5] * G[ai][2];
-      CG[1] = C[3] * G[ai][0] + C[1] * G[ai][1] + C[4] * G[ai][2];
-      CG[2] = C[5] * G[ai][0] + C[4] * G[ai][1] + C[2] * G[ai][2];
+      CG[0] = gaV * (C[0] * G[ai][0] + C[3] * G[ai][1] + C[5] * G[ai][2]);
+      CG[1] = gaV * (C[3] * G[ai][0] + C[1] * G[ai][1] + C[4] * G[ai][2]);
+      CG[2] = gaV * (C[5] * G[ai][0] + C[4] * G[ai][1] + C[2] * G[ai][2]);
     } else {
-      CG[0] = G[ai][0]; CG[1] = G[ai][1]; CG[2] = G[ai][2];
+      CG[0] = gaV * G[ai][0]; CG[1] = gaV * G[ai][1]; CG[2] = gaV * G[ai][2];
     }
     const double Za0 = zs * hv[ai][0], Za1 = zs * hv[ai][1], Za2 = zs * hv[ai][2];
     const double up0 = upf * hv[ai][0], up1 = upf * hv[ai][1], up2 = upf * hv[ai][2];
-    const double pu1 = (a.stab ? tJV * wv[ai] : 0.0) - pu0;
+    const double pu1 = twv[ai] - pu0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      const double cab = gaV * (CG[0] * G[b][0] + CG[1] * G[b][1] + CG[2] * G[b][2]);
+      const double cab = fma(CG[0], G[b][0], fma(CG[1], G[b][1], CG[2] * G[b][2]));
       const double eab = hv[ai][0] * hv[b][0] + hv[ai][1] * hv[b][1] + hv[ai][2] * hv[b][2];
       double K[4][4];
 #pragma unroll
@@ -491,19 +502,14 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           const double Zak = (k == 0) ? Za0 : ((k == 1) ? Za1 : Za2);
-          double t = hv[ai][i] * Xp[b][k] + qv[ai][i] * Yp[b][k] + hv[b][i] * Zak;
-          if (i == k) t += cab;
-          K[i][k] = t;
+          const double t0 = (i == k) ? fma(hv[b][i], Zak, cab) : hv[b][i] * Zak;
+          K[i][k] = fma(hv[ai][i], Xp[b][k], fma(qv[ai][i], Yp[b][k], t0));
         }
         K[i][3] = (i == 0) ? up0 : ((i == 1) ? up1 : up2);
       }
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        double t = pu1 * hv[b][k];
-        if (a.stab) t -= tJV * (eab * vv[k] + wv[b] * hv[ai][k]);
-        K[3][k] = t;
-      }
-      K[3][3] = ppc + (a.stab ? tJV * eab : 0.0);
+      for (int k = 0; k < 3; ++k) K[3][k] = fma(pu1, hv[b][k], -fma(eab, tvv[k], twv[b] * hv[ai][k]));
+      K[3][3] = fma(tJVs, eab, ppc);
       if constexpr (BUF) {
         double* eb = a.ebuf + (size_t)s * a.estride + 16 + 16 * (4 * ai + b);
 #pragma unroll
