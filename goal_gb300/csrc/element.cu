@@ -313,11 +313,16 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   if (MODE != MODE_NONE) {
     double Ru[4][3], Rp[4];
     if (!ERR) {
+      double TV[3][3];  // V J sigma
+#pragma unroll
+      for (int q = 0; q < 9; ++q) TV[q / 3][q % 3] = V * T[q / 3][q % 3];
+      const double rp0 = ((pval * inv_kappa) - dUdJ) * 0.25 * V;
+      const double rpw = a.stab ? tauJ * V : 0.0;
 #pragma unroll
       for (int n = 0; n < 4; ++n) {
 #pragma unroll
-        for (int i = 0; i < 3; ++i) Ru[n][i] = V * (T[i][0] * hv[n][0] + T[i][1] * hv[n][1] + T[i][2] * hv[n][2]);
-        Rp[n] = ((pval * inv_kappa) - dUdJ) * 0.25 * V + (a.stab ? tauJ * wv[n] * V : 0.0);
+        for (int i = 0; i < 3; ++i) Ru[n][i] = fma(TV[i][0], hv[n][0], fma(TV[i][1], hv[n][1], TV[i][2] * hv[n][2]));
+        Rp[n] = fma(rpw, wv[n], rp0);
       }
     } else {
       // DWR weights: z_diff phi_a (momentum, pressure), z_coarse phi_a (stabilization)
