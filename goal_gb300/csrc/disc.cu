@@ -97,6 +97,16 @@ __device__ __forceinline__ int lower_bound_dev(const int* a, int n, int key) {
   return lo;
 }
 
+// off-diagonal blocks in block order: block k of row n (k != diag[n]) goes to
+// position k - n - (k > diag[n]) (one diagonal block per earlier row)
+__global__ void k_offd(int N, const int* brow_ptr, const int* diag, int* offd) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    const int dn = diag[n];
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k)
+      if (k != dn) offd[k - n - (k > dn ? 1 : 0)] = k;
+  }
+}
+
 __global__ void k_diag(int N, const int* brow_ptr, const int* bcol, int* diag) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
     int b = brow_ptr[n];
@@ -315,6 +325,9 @@ void Disc::build() {
   GOAL_CHECK_LAUNCH();
   diag.alloc(N);
   k_diag<<<grid_for(N, 256), 256, 0, s>>>(N, brow_ptr.ptr, bcol.ptr, diag.ptr);
+  GOAL_CHECK_LAUNCH();
+  offd.alloc(nnzb - N);
+  k_offd<<<grid_for(N, 256), 256, 0, s>>>(N, brow_ptr.ptr, diag.ptr, offd.ptr);
   GOAL_CHECK_LAUNCH();
 
   // colouring

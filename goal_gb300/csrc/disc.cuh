@@ -85,6 +85,9 @@ struct Disc {
   // entries 16*s + (4a+b); node n sums element rows nlist[nptr[n]..nptr[n+1])
   // with entries 4*s + a. Both are ordered by element, so sums are deterministic.
   DevBuf<int> bptr, blist, nptr, nlist;
+  // off-diagonal block ids (nnzb - N), so that the gather can treat the
+  // diagonal blocks (many contributions) apart from the others (few)
+  DevBuf<int> offd;
 
   std::map<std::string, std::unique_ptr<NodeSet>> node_sets;
   std::map<std::string, std::unique_ptr<SideSet>> side_sets;

@@ -673,14 +673,18 @@ __device__ __forceinline__ void load_contrib(const double* __restrict__ ebuf, in
 // blocks in element order (4 threads per block, one per row); TRANSPOSE
 // accumulates the element blocks transposed (ADJOINT mode stores dR/du^T).
 // Contributions are fetched four at a time (independent loads in flight),
-// then added in element order.
+// then added in element order. The blocks come from a list (ks[0..count)):
+// one launch for the off-diagonal blocks (a few contributions each) and one
+// for the diagonal blocks (one per incident element), so that the threads of
+// a warp do equal work.
 template <bool TRANSPOSE>
-__global__ void __launch_bounds__(256) k_gather_blocks(int nnzb, const int* __restrict__ bptr,
-                                                       const int* __restrict__ blist, const double* __restrict__ ebuf,
-                                                       int estride, double* __restrict__ A, int accumulate) {
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4ll * nnzb;
+__global__ void __launch_bounds__(256) k_gather_blocks(int count, const int* __restrict__ ks,
+                                                       const int* __restrict__ bptr, const int* __restrict__ blist,
+                                                       const double* __restrict__ ebuf, int estride,
+                                                       double* __restrict__ A, int accumulate) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4ll * count;
        t += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(t >> 2), r = (int)(t & 3);
+    const int k = __ldg(ks + (t >> 2)), r = (int)(t & 3);
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     if (accumulate) ld4(A + 16ll * k + 4 * r, a0, a1, a2, a3);
     const int c1 = __ldg(bptr + k + 1);
@@ -907,13 +911,19 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
                                                                         m.ebuf.ptr, a.estride, s->R.ptr, acc);
     GOAL_CHECK_LAUNCH();
     if (c.jacobian) {
-      if (c.mode == MODE_ADJOINT)
-        k_gather_blocks<true><<<grid_for(4ll * d.nnzb, 256), 256, 0, st>>>(d.nnzb, d.bptr.ptr, d.blist.ptr, m.ebuf.ptr,
-                                                                           a.estride, s->A.ptr, acc);
-      else
-        k_gather_blocks<false><<<grid_for(4ll * d.nnzb, 256), 256, 0, st>>>(d.nnzb, d.bptr.ptr, d.blist.ptr,
-                                                                            m.ebuf.ptr, a.estride, s->A.ptr, acc);
-      GOAL_CHECK_LAUNCH();
+      const int noff = d.nnzb - d.num_nodes;
+      const int* lists[2] = {d.offd.ptr, d.diag.ptr};
+      const int counts[2] = {noff, d.num_nodes};
+      for (int q = 0; q < 2; ++q) {
+        if (counts[q] <= 0) continue;
+        if (c.mode == MODE_ADJOINT)
+          k_gather_blocks<true><<<grid_for(4ll * counts[q], 256), 256, 0, st>>>(
+              counts[q], lists[q], d.bptr.ptr, d.blist.ptr, m.ebuf.ptr, a.estride, s->A.ptr, acc);
+        else
+          k_gather_blocks<false><<<grid_for(4ll * counts[q], 256), 256, 0, st>>>(
+              counts[q], lists[q], d.bptr.ptr, d.blist.ptr, m.ebuf.ptr, a.estride, s->A.ptr, acc);
+        GOAL_CHECK_LAUNCH();
+      }
     }
   }
   if (buf && c.jacobian && c.qoi != QOI_NONE && s) {
