@@ -125,16 +125,15 @@ __global__ void k_sum_log(int N, const float* x, double* part) {
 }
 __global__ void k_sub_log_mean(int N, int nb, const double* part, float* x) {
   __shared__ double mean;
-  if (threadIdx.x == 0) {
-    KSum acc;
-    for (int i = 0; i < nb; ++i) {
-      KSum t;
-      t.s = part[2 * i];
-      t.c = part[2 * i + 1];
-      acc.add(t);
-    }
-    mean = acc.value() / N;
+  KSum acc;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    KSum t;
+    t.s = part[2 * i];
+    t.c = part[2 * i + 1];
+    acc.add(t);
   }
+  acc = block_reduce(acc);
+  if (threadIdx.x == 0) mean = acc.value() / N;
   __syncthreads();
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
     x[20ll * n + 16] = (float)((double)x[20ll * n + 16] - mean);
