@@ -259,3 +259,66 @@ def test_assembly_is_deterministic_and_overwrite_matches_accumulate(meshes, colo
     # both scatter strategies assemble the same matrix (up to summation order)
     api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, colored=not colored)
     assert np.abs(s.dRdu_bsr() - A1).max() <= 1e-13 * np.abs(A1).max()
+
+
+def _gpu_with_mats(mesh, model, mats, u, p, st, stabilization=True):
+    d = api.Disc(mesh)
+    m = api.Mechanics(d, model, [mt.row() for mt in mats], stabilization=stabilization)
+    U = np.zeros((mesh.num_nodes, 4))
+    U[:, :3] = u
+    U[:, 3] = p
+    m.set_solution(U.ravel())
+    m.set_state(api.FP_OLD, st.Fp_old)
+    m.set_state(api.EQPS_OLD, st.eqps_old)
+    m.set_state(api.FP, st.Fp)
+    m.set_state(api.EQPS, st.eqps)
+    m.set_state(api.SIGMA, st.sigma)
+    return d, m, api.SolInfo(d)
+
+
+@pytest.mark.parametrize("model", [O.NEOHOOKEAN, O.J2])
+@pytest.mark.parametrize("stabilization", [True, False])
+def test_heterogeneous_materials(model, stabilization):
+    """Per-element-set materials (four regions of a graded block, different E,
+    nu, Y, c0), with and without the stabilization term."""
+    mesh = graded_block(2500, seed=5, regions=4)
+    assert len(np.unique(mesh.elem_set)) == 4
+    rng = np.random.default_rng(3)
+    mats = [O.Material(float(rng.lognormal(np.log(1000.0), 0.5)), float(rng.uniform(0.2, 0.45)), K=100.0,
+                       Y=float(rng.uniform(5.0, 30.0)), c0=float(rng.uniform(0.5, 2.0))) for _ in range(4)]
+    u, p, st = random_state(mesh, 17, 0.02 if model == O.NEOHOOKEAN else 5e-3, model)
+    d, m, s = _gpu_with_mats(mesh, model, mats, u, p, st, stabilization)
+    api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=True)
+    g = O.csr_graph(mesh.num_nodes, mesh.tets)
+    R = np.zeros(4 * mesh.num_nodes)
+    vals = np.zeros(len(g[1]))
+    ost = st.copy()
+    _, npl = O.assemble(mesh, model, mats, u, p, ost, mode=O.PRIMAL, fad=True, save=True, graph=g, R=R, vals=vals,
+                        stabilization=stabilization)
+    assert rel_vec(s.R, R) < RTOL
+    assert rel_rows(s.dRdu_csr(), vals, g[0]) < RTOL
+    if model == O.J2:
+        assert npl > 0
+        assert rel_vec(m.get_state(api.FP), ost.Fp) < RTOL
+
+
+def test_single_element_and_single_colour():
+    """The smallest mesh: one tet (one colour, one 16x16 element matrix)."""
+    from goal_gb300.mesh import Mesh
+    coords = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+    tets = np.array([[0, 1, 2, 3]], np.int32)
+    mesh = Mesh(coords=coords, tets=tets, elem_set=np.zeros(1, np.int32), elem_set_names=["one"],
+                node_sets={"xmin": np.array([0, 2, 3], np.int32)}, side_sets={})
+    for model in (O.NEOHOOKEAN, O.J2):
+        u, p, st = random_state(mesh, 2, 0.05, model)
+        d, m, s = make_gpu(mesh, model, u, p, st)
+        assert d.num_colors == 1
+        api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False)
+        g = O.csr_graph(mesh.num_nodes, mesh.tets)
+        R = np.zeros(16)
+        vals = np.zeros(len(g[1]))
+        O.assemble(mesh, model, [MATS[model]], u, p, st.copy(), mode=O.PRIMAL, fad=True, save=False, graph=g, R=R,
+                   vals=vals)
+        assert len(vals) == 256
+        assert rel_vec(s.R, R) < RTOL
+        assert rel_rows(s.dRdu_csr(), vals, g[0]) < RTOL
