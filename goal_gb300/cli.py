@@ -9,11 +9,13 @@ and the regression check (src/goal_regression.cpp:14-23), with goal's log lines
 (`J(uH) = %.15e`, `||R||`, linear iterations).
 
 ``nested`` is GoalNested (src/main_nested.cpp:128-151) for adjoint mode
-"uniform": per load step the primal solve, the functional and the output, then
-NestedAdjoint::run on the uniformly refined mesh (`z.R = %.15e`,
-`|J(u)-J(uh)| < %.15e`) and the isotropic target size field for the next
-cycle (src/goal_size_field.cpp). The remeshing to that size (SCOREC ma::adapt)
-is not available, so the driver runs adaptation cycle 0 only.
+"uniform": per load step and adaptation cycle the primal solve, the
+functional and the output; before every cycle but the last, NestedAdjoint::run
+on the uniformly refined mesh (`z.R = %.15e`, `|J(u)-J(uh)| < %.15e`), the
+isotropic target size field (src/goal_size_field.cpp) for "target elems" x
+"target growth"^(cycle-1), and the refinement of the mesh to that size with
+the solution and states carried over (goal_gb300.adapt; goal remeshes with
+SCOREC ma::adapt, which also coarsens -- this refines only).
 
 3D meshes in SCOREC SMB v5 with their .dmg model and association file, the
 package's .npz mesh file, or a restart directory written with "write native";
@@ -65,25 +67,16 @@ class _Setup:
             mesh = load_npz(mesh_file, list(mech_p["materials"].keys()))
         else:
             mesh = smb.load(_resolve(base, dp["geom file"]), mesh_file, _resolve(base, dp["assoc file"]))
-        self.mesh = mesh
-        model = {"neohookean": api.NEOHOOKEAN, "J2": api.J2}.get(mech_p["model"])
-        if model is None:
+        self.model = {"neohookean": api.NEOHOOKEAN, "J2": api.J2}.get(mech_p["model"])
+        if self.model is None:
             raise ValueError(f"unknown model: {mech_p['model']}")
-        mats = []
-        for es in mesh.elem_set_names:
-            m = mech_p["materials"][es]
-            mats.append([float(m["E"]), float(m["nu"]), float(m.get("K", 0.0)), float(m.get("Y", 0.0)),
-                         float(m.get("c0", 0.0))])
-        self.d = api.Disc(mesh)
-        self.mech = api.Mechanics(self.d, model, mats, stabilization=bool(mech_p.get("stabilization", True)))
-        if self.restart:
-            output.apply_restart(self.mech, *self.restart)
-        self.s = api.SolInfo(self.d)
         self.dbcs = [(int(v[0]), str(v[1]), str(v[2])) for v in p.get("dirichlet bcs", {}).values()]
         self.tbcs = [tuple(str(x) for x in v) for v in p.get("traction bcs", {}).values()]
         if p.get("inward bcs"):
             raise ValueError("inward bcs are not supported")
-        self.bcs = api.Bcs(self.d, self.dbcs, self.tbcs)
+        self.build(mesh)
+        if self.restart:
+            output.apply_restart(self.mech, *self.restart)
         fp = p["functional"]
         self.qoi_name = fp["type"]
         self.qoi = {"avg disp": api.QOI_AVG_DISP, "max vm": api.QOI_KS_VM}.get(fp["type"])
@@ -95,6 +88,39 @@ class _Setup:
         self.newton_iters = int(la["nonlinear max iters"])
         self.newton_tol = float(la["nonlinear tolerance"])
         self.output = output.Output(p.get("output", {}), mesh, self.mech, os.getcwd())
+
+    def build(self, mesh):
+        """Disc::build_data, Mechanics, SolInfo and BCs on ``mesh``."""
+        mech_p = self.p["mechanics"]
+        mats = []
+        for es in mesh.elem_set_names:
+            m = mech_p["materials"][es]
+            mats.append([float(m["E"]), float(m["nu"]), float(m.get("K", 0.0)), float(m.get("Y", 0.0)),
+                         float(m.get("c0", 0.0))])
+        self.mesh = mesh
+        self.d = api.Disc(mesh)
+        self.mech = api.Mechanics(self.d, self.model, mats, stabilization=bool(mech_p.get("stabilization", True)))
+        self.s = api.SolInfo(self.d)
+        self.bcs = api.Bcs(self.d, self.dbcs, self.tbcs)
+        if hasattr(self, "output"):
+            self.output.mesh, self.output.mech = mesh, self.mech
+
+    def adapt_to(self, size, ratio=1.5):
+        """Refines to the target size field and moves the solution and the
+        states onto the refined mesh (the remeshing of Solver::adapt,
+        src/main_nested.cpp:106-126, with goal's field transfer)."""
+        from . import adapt
+        U = self.mech.get_solution().reshape(-1, 4)
+        states = {n: self.mech.get_state(w) for n, w, _ in output.STATE_FIELDS
+                  if self.model == api.J2 or w == api.SIGMA}
+        mesh, parents, origin = adapt.refine_to_size(self.mesh, size, ratio=ratio)
+        U2 = adapt.transfer_nodal(U, parents)
+        st2 = adapt.transfer_states(states, origin)
+        self.build(mesh)
+        self.mech.set_solution(U2.ravel())
+        ids = {n: w for n, w, _ in output.STATE_FIELDS}
+        for k, v in st2.items():
+            self.mech.set_state(ids[k], v)
 
     @staticmethod
     def _linear(la):
@@ -151,26 +177,34 @@ def nested(path: str, out=print) -> dict:
     if mode != "uniform":
         raise ValueError(f"adjoint mode {mode!r} is not supported (uniform only)")
     ad = S.p.get("adaptation", {})
-    target = int(ad.get("target elems", S.mesh.num_elems))
+    target0 = int(ad.get("target elems", S.mesh.num_elems))
+    growth = float(ad.get("target growth", 1.0))
     cycles = int(ad.get("adapt cycles", 1))
     aprm = S._linear(S.p.get("adjoint linear algebra", S.p["primal linear algebra"]))
     J = None
-    last = {}
+    last = {"cycles": []}
     for step, t_now, t_old in S.steps():
-        J = S.primal_step(step, t_now, t_old, out)
-        S.output.write(t_now, 0)
-        if cycles > 0:
-            na = api.NestedAdjoint(S.mech, S.dbcs, S.tbcs)
-            out(f"*** adjoint error estimation: {na.disc.num_dofs} dofs")
-            out(f"*** at time: {t_now:f}")
-            r = na.run(S.qoi, S.rho, t_now, t_old, aprm)
-            out(f" > z.R = {r['eta']:.15e}")
-            out(f" > |J(u)-J(uh)| < {r['bound']:.15e}")
-            size = api.size_field(S.d, r["base_error"], target)
-            out(f" > isotropic target size field: {size.min():e} .. {size.max():e}")
-            out("*** adaptation: remeshing to the size field is not available; continuing on this mesh")
-            last = dict(eta=r["eta"], bound=r["bound"], base_error=r["base_error"], size=size)
-            na.close()
+        for cycle in range(cycles + 1):
+            J = S.primal_step(step, t_now, t_old, out)
+            S.output.write(t_now, cycle)
+            rec = {"step": step, "cycle": cycle, "elements": S.mesh.num_elems, "J": J}
+            if cycle < cycles:
+                na = api.NestedAdjoint(S.mech, S.dbcs, S.tbcs)
+                out(f"*** adjoint error estimation: {na.disc.num_dofs} dofs")
+                out(f"*** at time: {t_now:f}")
+                r = na.run(S.qoi, S.rho, t_now, t_old, aprm)
+                out(f" > z.R = {r['eta']:.15e}")
+                out(f" > |J(u)-J(uh)| < {r['bound']:.15e}")
+                na.close()
+                out("*** adaptation")
+                out(f"*** at step: ({step})")
+                out(f"*** at cycle: ({cycle})")
+                target = int(target0 * growth ** (cycle - 1.0))
+                size = api.size_field(S.d, r["base_error"], max(1, target))
+                S.adapt_to(size)
+                out(f" > refined to {S.mesh.num_elems} elements (target {target})")
+                rec.update(eta=r["eta"], bound=r["bound"], refined_elements=S.mesh.num_elems)
+            last["cycles"].append(rec)
         S.mech.update_states()
     S.regression(J, out)
     last["J"] = J

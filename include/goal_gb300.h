@@ -110,6 +110,29 @@ int goal_nested_parent_edges(goal_disc nested, int* edges);
  * G = sum |e|^(6/5) and h_e the root mean square edge length. */
 int goal_size_field(goal_disc d, const double* elem_error, int target, double* vtx_size);
 
+/* Refinement to the target size, the refinement half of goal's adaptation
+ * loop (src/main_nested.cpp:106-126, where SCOREC ma::adapt remeshes; that
+ * library is not part of the reference). Conforming longest-edge-propagation
+ * (LEPP) bisection on the host: every live tet with an edge longer than
+ * ratio x (mean target size of its end points) is refined until none is left
+ * (or max_elems / max_passes is reached). New nodes sit at edge midpoints and
+ * take the mean target size of the edge's end points. Side triangles
+ * (tris[3*num_sides], tri_set[num_sides]) are split with their edges.
+ * create: the mesh; refine: vtx_size[num_nodes] -> sizes[0..2] = nodes,
+ * elements, side triangles of the refined mesh; get: coords[3*nodes],
+ * node_parents[2*nodes] (edge end points of new nodes, -1 -1 for original
+ * nodes; new nodes follow the original ones in creation order),
+ * tets[4*elements], elem_origin[elements] (original element of each tet),
+ * tris/tri_set (may be NULL). */
+typedef struct goal_refiner_s* goal_refiner;
+int goal_refiner_create(int num_nodes, const double* coords, int num_elems, const int* tets, int num_sides,
+                        const int* tris, const int* tri_set, goal_refiner* out);
+int goal_refiner_refine(goal_refiner r, const double* vtx_size, double ratio, long long max_elems, int max_passes,
+                        long long* sizes);
+int goal_refiner_get(goal_refiner r, double* coords, int* node_parents, int* tets, int* elem_origin, int* tris,
+                     int* tri_set);
+int goal_refiner_destroy(goal_refiner r);
+
 /* ---------------------------------------------------------------- Mechanics
  * goal::create_mechanics (src/goal_mechanics.hpp:50). materials holds, per
  * element set, E, nu, K, Y, c0 (K and Y are read by J2 only). States start as
