@@ -49,6 +49,9 @@ def _args():
     ap.add_argument("--adjoint-n", type=int, default=40, help="base mesh of the adjoint-solve leg (0: skip)")
     ap.add_argument("--learned-eval", type=int, default=20,
                     help="held-out seeds of the learned-preconditioner study (0: skip)")
+    ap.add_argument("--adaptive-cycles", type=int, default=2,
+                    help="cycles of the goal-oriented adaptive loop on the graded block (0: skip)")
+    ap.add_argument("--adaptive-start", type=int, default=100000, help="elements of the adaptive loop's first mesh")
     return ap.parse_args()
 
 
@@ -443,6 +446,84 @@ def learned_eval_leg(api, held_out, train_problems=8, train_target=20000, eval_t
     return out
 
 
+# ------------------------------------------------------------------ adaptive loop
+def adaptive_leg(api, cycles, start, growth=2.0, seed=7):
+    """The goal-oriented adaptive loop (GoalNested, src/main_nested.cpp:128-151)
+    on the graded block of the learned-preconditioner study (seed 7: J2, 8
+    material regions), one load step (u_x = 0.04 on x=4), KS von Mises
+    (rho = 20): per cycle the Newton solve, five timed R+J assemblies, the
+    nested adjoint solved to 1e-10 with FP32-inner / FP64-outer FGMRES (plain
+    block-Jacobi, then the network trained on this cycle's Newton Jacobian),
+    the DWR estimate, the size field for growth x elements, and the refinement
+    with the fields carried over."""
+    import torch
+    from goal_gb300 import adapt
+    from goal_gb300.mesh import graded_block
+    rng = np.random.default_rng(1000 + seed)
+    mesh = graded_block(start, seed=seed, regions=BLOCK_REGIONS)
+    mats = [[float(rng.lognormal(np.log(1000.0), 0.5)), float(rng.uniform(0.2, 0.45)), 100.0,
+             float(rng.uniform(50.0, 300.0)), 1.0] for _ in range(BLOCK_REGIONS)]
+    dbcs = [(0, "xmin", "0.0"), (1, "xmin", "0.0"), (2, "xmin", "0.0"), (0, "xmax", "0.04*t")]
+    newton_prm = api.solve_params(tolerance=1e-10, precision=api.MIXED, inner_iters=30, krylov_size=30, max_iters=3000)
+    mix = dict(krylov_size=30, tolerance=1e-10, max_iters=3000, precision=api.MIXED, inner_iters=30)
+    U = states = None
+    out = []
+    for cycle in range(cycles + 1):
+        d = api.Disc(mesh)
+        m = api.Mechanics(d, api.J2, mats)
+        if U is not None:
+            m.set_solution(U.ravel())
+            for k, v in states.items():
+                m.set_state({"sigma": api.SIGMA, "Fp": api.FP, "Fp_old": api.FP_OLD, "eqps": api.EQPS,
+                             "eqps_old": api.EQPS_OLD}[k], v)
+        s = api.SolInfo(d)
+        bcs = api.Bcs(d, dbcs, [])
+        t0 = time.perf_counter()
+        newton = api.primal_solve(m, s, bcs, 1.0, 0.0, 15, 1e-8, newton_prm)
+        t_newton = time.perf_counter() - t0
+        J = api.assemble(m, None, api.NONE, jacobian=False, save_states=False, qoi=api.QOI_KS_VM, rho=20.0)
+        stream = torch.cuda.ExternalStream(d.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False)
+        e0.record(stream)
+        for _ in range(5):
+            api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        rec = {"cycle": cycle, "elements": mesh.num_elems, "dofs": d.num_dofs, "newton_iters": newton["iters"],
+               "newton_seconds": t_newton, "J": J, "assembly_elem_per_s": mesh.num_elems / (ms * 1e-3),
+               "assembly_ms": ms}
+        if cycle < cycles:
+            api.set_jac_dbcs(m, s, bcs, 1.0)
+            net = api.Learned(seed=0)
+            net.train([s], epochs=60, lr=2e-3, num_probes=8)
+            na = api.NestedAdjoint(m, dbcs, [])
+            r0 = na.run(api.QOI_KS_VM, 20.0, 1.0, 0.0, api.solve_params(**mix))
+            net.attach(na.si_handle())
+            r1 = na.run(api.QOI_KS_VM, 20.0, 1.0, 0.0,
+                        api.solve_params(precond=api.PRECOND_LEARNED, learned_cap=1500, **mix))
+            rec.update(nested_dofs=na.disc.num_dofs,
+                       adjoint_mixed={"seconds": r0["seconds_solve"], "outer_iters": r0["solve"]["iters"]},
+                       adjoint_learned_mixed={"seconds": r1["seconds_solve"], "outer_iters": r1["solve"]["iters"],
+                                              "fell_back": r1["solve"]["fell_back"]},
+                       eta=r1["eta"], bound=r1["bound"], eta_rel_diff=abs(r1["eta"] - r0["eta"]) / abs(r0["eta"]))
+            target = int(mesh.num_elems * growth)
+            size = api.size_field(d, r1["base_error"], target)
+            na.close()
+            U = m.get_solution().reshape(-1, 4)
+            states = {"sigma": m.get_state(api.SIGMA), "Fp": m.get_state(api.FP), "Fp_old": m.get_state(api.FP_OLD),
+                      "eqps": m.get_state(api.EQPS), "eqps_old": m.get_state(api.EQPS_OLD)}
+            t1 = time.perf_counter()
+            mesh, parents, origin = adapt.refine_to_size(mesh, size)
+            rec["refine_seconds"] = time.perf_counter() - t1
+            rec["target"] = target
+            U = adapt.transfer_nodal(U, parents)
+            states = adapt.transfer_states(states, origin)
+        out.append(rec)
+    return out
+
+
 # ------------------------------------------------------------------ replicas
 def max_over_ranks(x: float, world: int, device: str) -> float:
     """The slowest rank's time: every rank runs the same replica workload (no
@@ -600,6 +681,11 @@ def main():
             line["learned_eval"] = learned_eval_leg(api, a.learned_eval)
         except Exception as exc:
             line["learned_eval"] = {"error": str(exc)[:300]}
+    if a.adaptive_cycles > 0:
+        try:
+            line["adaptive_loop"] = adaptive_leg(api, a.adaptive_cycles, a.adaptive_start)
+        except Exception as exc:
+            line["adaptive_loop"] = {"error": str(exc)[:300]}
     if a.adjoint_n > 0:
         try:
             line["adjoint_solve"] = adjoint_leg(a.adjoint_n, api)
