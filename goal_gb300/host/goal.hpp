@@ -304,4 +304,46 @@ class NestedAdjoint {
   long long base_elems_ = 0;
 };
 
+// get_iso_target_size (src/goal_size_field.cpp:139-151): per-node target sizes
+inline std::vector<double> get_iso_target_size(Disc& d, const std::vector<double>& elem_error, int target) {
+  std::vector<double> size(d.get_num_nodes());
+  check(goal_size_field(d.handle(), elem_error.data(), target, size.data()));
+  return size;
+}
+
+// The refinement half of Solver::adapt (src/main_nested.cpp:106-126): the mesh
+// refined until no edge is longer than ratio x its target size, with the node
+// parents (new nodes at edge midpoints, after the old nodes) and the original
+// element of every new element, for the field transfer.
+struct RefinedMesh {
+  std::vector<double> coords;
+  std::vector<int> tets, elem_origin, node_parents, tris, tri_set;
+};
+inline RefinedMesh refine_to_size(const std::vector<double>& coords, const std::vector<int>& tets,
+                                  const std::vector<int>& tris, const std::vector<int>& tri_set,
+                                  const std::vector<double>& vtx_size, double ratio = 1.5,
+                                  long long max_elems = 50000000, int max_passes = 64) {
+  goal_refiner r = nullptr;
+  check(goal_refiner_create((int)(coords.size() / 3), coords.data(), (int)(tets.size() / 4), tets.data(),
+                            (int)tri_set.size(), tris.data(), tri_set.data(), &r));
+  long long sizes[3];
+  int rc = goal_refiner_refine(r, vtx_size.data(), ratio, max_elems, max_passes, sizes);
+  if (rc != GOAL_OK) {
+    goal_refiner_destroy(r);
+    check(rc);
+  }
+  RefinedMesh m;
+  m.coords.resize(3 * sizes[0]);
+  m.node_parents.resize(2 * sizes[0]);
+  m.tets.resize(4 * sizes[1]);
+  m.elem_origin.resize(sizes[1]);
+  m.tris.resize(3 * sizes[2]);
+  m.tri_set.resize(sizes[2]);
+  rc = goal_refiner_get(r, m.coords.data(), m.node_parents.data(), m.tets.data(), m.elem_origin.data(),
+                        m.tris.data(), m.tri_set.data());
+  goal_refiner_destroy(r);
+  check(rc);
+  return m;
+}
+
 }  // namespace goal

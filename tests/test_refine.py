@@ -101,3 +101,19 @@ def test_deterministic_and_states_follow_parents():
     t = adapt.transfer_nodal(lin, parents)[:, 0]
     assert np.allclose(t, out.coords @ np.array([1.0, -2.0, 0.5]) + 3.0, atol=1e-12)
     assert adapt.transfer_nodal(U, parents).shape == (out.num_nodes, 4)
+
+
+def test_cpp_mirror_refines(tmp_path):
+    """goal::refine_to_size in the C++ mirror, compiled with g++ against the C
+    ABI (the refiner is host code: no GPU needed)."""
+    import os
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    from goal_gb300 import lib
+    lib()  # built in-tree
+    exe = tmp_path / "refine_check"
+    subprocess.check_call(["g++", "-O2", "-std=c++17", os.path.join(root, "tests", "cpp", "refine_check.cpp"),
+                           "-I", os.path.join(root, "include"), "-L", os.path.join(root, "goal_gb300"),
+                           "-lgoal_gb300", f"-Wl,-rpath,{os.path.join(root, 'goal_gb300')}", "-o", str(exe)])
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
