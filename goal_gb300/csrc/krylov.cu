@@ -343,14 +343,36 @@ __global__ void k_norm_fin(int nbx, const double* part, GState* st, double* H, i
 }
 
 template <typename T>
+struct Vec4Store;
+template <>
+struct Vec4Store<double> {
+  static __device__ __forceinline__ void store(double* p, double a, double b, double c, double d) {
+    double4_32a v;
+    v.x = a; v.y = b; v.z = c; v.w = d;
+    *reinterpret_cast<double4_32a*>(p) = v;
+  }
+};
+template <>
+struct Vec4Store<float> {
+  static __device__ __forceinline__ void store(float* p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+  }
+};
+
+// V_{j+1} = w / H[j+1, j], four entries per thread (n = 4 x nodes; every
+// column starts on a 32-byte boundary)
+template <typename T>
 __global__ void k_normalize(long long n, T* V, long long ld, const T* w, const GState* st, const double* H, int ldh) {
   if (st->done) return;
   const int j = st->j;
   const double h = H[j + 1 + (long long)ldh * j];
   const T inv = (h > 0.0) ? (T)(1.0 / h) : T(0);
   T* v = V + (long long)(j + 1) * ld;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    v[i] = w[i] * inv;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; 4 * q < n; q += (long long)gridDim.x * blockDim.x) {
+    T a, b, c, d;
+    Vec4<T>::load(w + 4 * q, a, b, c, d);
+    Vec4Store<T>::store(v + 4 * q, a * inv, b * inv, c * inv, d * inv);
+  }
 }
 
 // Applies the previous rotations to the new Hessenberg column (staged in
@@ -694,7 +716,7 @@ void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, doubl
     case 4: orth_passes<T, 4>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
     default: orth_passes<T, 8>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
   }
-  k_normalize<T><<<vec_grid(n), 256, 0, s>>>(n, V, n, w, st, H, ldh);
+  k_normalize<T><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st, H, ldh);
   GOAL_CHECK_LAUNCH();
   k_givens<<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
   GOAL_CHECK_LAUNCH();
