@@ -601,13 +601,16 @@ __global__ void k_inner_blocks(int N, const double* __restrict__ Dinv, const dou
 
 int spmv_grid(int N) { return grid_for((long long)N * 4, 256, kSMs * 16); }
 int vec_grid(long long n) { return grid_for(n, 256, kSMs * 8); }
-// Rows per thread of the orthogonalization kernels: enough blocks to fill the
-// GPU (8 per SM for FP32, 4 per SM for FP64, whose reductions cost FP64
-// instructions and so want longer slabs), at most kMaxRows.
+// Rows per thread of the orthogonalization kernels. FP64: always the longest
+// slab, because the per-block reductions cost FP64 instructions (measured on
+// the 530k-dof nested adjoint: 141 us per multidot pass with 2 rows per thread
+// against 64 us with 8). FP32: enough blocks for about eight per SM, at least
+// two and at most kMaxRows rows per thread.
 template <typename T>
 int slab_rows(long long n) {
-  const long long target = (std::is_same<T, float>::value ? 8ll : 4ll) * kSMs * 256;
-  int r = 1;
+  if (!std::is_same<T, float>::value) return kMaxRows;
+  const long long target = 8ll * kSMs * 256;
+  int r = 2;
   while (r < kMaxRows && n >= 2ll * r * target) r *= 2;
   return r;
 }
