@@ -25,6 +25,7 @@ struct GState {
   double wb2;   // |w|^2 before orthogonalization
   double res;   // |g[j]| residual estimate
   double beta;  // initial residual norm of the cycle
+  double hnext; // |w| after a single-pass orthogonalization (read by the normalization)
 };
 
 constexpr int kMaxM = 256;
@@ -412,6 +413,71 @@ __global__ void k_givens(GState* st, double* H, int ldh, double* cs, double* sn,
   for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) h[i] = sh[i];
 }
 
+// Single-pass orthogonalization: |w| from the block partials (H[j+1, j] and
+// hnext), then the Givens step, in one block.
+__global__ void k_norm_givens(int nbx, const double* part, GState* st, double* H, int ldh, double* cs, double* sn,
+                              double* g, int jmax, double tol_abs) {
+  if (st->done) return;
+  const int j = st->j;
+  double v = 0.0;
+  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
+  __shared__ double sm[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double* h = H + (long long)ldh * j;
+  __shared__ double sh[kMaxM + 2], scs[kMaxM + 1], ssn[kMaxM + 1];
+  if (threadIdx.x == 0) {
+    double s2 = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s2 += sm[k];
+    const double nrm = sqrt(s2);
+    st->hnext = nrm;
+    sh[j + 1] = nrm;
+  }
+  for (int i = threadIdx.x; i <= j; i += blockDim.x) sh[i] = h[i];
+  for (int i = threadIdx.x; i < j; i += blockDim.x) {
+    scs[i] = cs[i];
+    ssn[i] = sn[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < j; ++i) {
+      const double t = scs[i] * sh[i] + ssn[i] * sh[i + 1];
+      sh[i + 1] = -ssn[i] * sh[i] + scs[i] * sh[i + 1];
+      sh[i] = t;
+    }
+    const double a = sh[j], b = sh[j + 1];
+    const double r = hypot(a, b);
+    double c = 1.0, s = 0.0;
+    if (r > 0.0) { c = a / r; s = b / r; }
+    cs[j] = c;
+    sn[j] = s;
+    sh[j] = r;
+    sh[j + 1] = 0.0;
+    g[j + 1] = -s * g[j];
+    g[j] = c * g[j];
+    st->res = fabs(g[j + 1]);
+    st->j = j + 1;
+    if (st->res <= tol_abs || st->j >= jmax || b == 0.0 || !(st->res == st->res)) st->done = 1;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) h[i] = sh[i];
+}
+
+// V_j = w / hnext after k_norm_givens advanced j
+template <typename T>
+__global__ void k_normalize_next(long long n, T* V, long long ld, const T* w, const GState* st) {
+  if (st->done) return;
+  const double h = st->hnext;
+  const T inv = (h > 0.0) ? (T)(1.0 / h) : T(0);
+  T* v = V + (long long)st->j * ld;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; 4 * q < n; q += (long long)gridDim.x * blockDim.x) {
+    T a, b, c, d;
+    Vec4<T>::load(w + 4 * q, a, b, c, d);
+    Vec4Store<T>::store(v + 4 * q, a * inv, b * inv, c * inv, d * inv);
+  }
+}
+
 __global__ void k_backsolve(const GState* st, const double* H, int ldh, const double* g, double* y) {
   const int k = st->j;
   for (int i = k - 1; i >= 0; --i) {
@@ -703,8 +769,10 @@ void orth_passes(long long n, T* V, T* w, GState* st, double* H, int ldh, double
     GOAL_CHECK_LAUNCH();
     k_update<T, R><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
     GOAL_CHECK_LAUNCH();
-    k_norm_fin<<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
-    GOAL_CHECK_LAUNCH();
+    if (passes > 1) {
+      k_norm_fin<<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
+      GOAL_CHECK_LAUNCH();
+    }
   }
 }
 
@@ -719,10 +787,19 @@ void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, doubl
     case 4: orth_passes<T, 4>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
     default: orth_passes<T, 8>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
   }
-  k_normalize<T><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st, H, ldh);
-  GOAL_CHECK_LAUNCH();
-  k_givens<<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
-  GOAL_CHECK_LAUNCH();
+  if (passes > 1) {
+    k_normalize<T><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st, H, ldh);
+    GOAL_CHECK_LAUNCH();
+    k_givens<<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
+    GOAL_CHECK_LAUNCH();
+  } else {
+    // one pass: norm and Givens in one block, then V_{j+1} = w / |w|
+    const int nbx = slab_grid(n, slab_rows<T>(n));
+    k_norm_givens<<<1, 256, 0, s>>>(nbx, red + (size_t)(kMaxM + 2) * nbx, st, H, ldh, cs, sn, g, jmax, tol_abs);
+    GOAL_CHECK_LAUNCH();
+    k_normalize_next<T><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st);
+    GOAL_CHECK_LAUNCH();
+  }
 }
 
 double read_norm(long long n, const double* x, Krylov& K) {
