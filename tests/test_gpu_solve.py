@@ -106,8 +106,8 @@ def _primal_problem(n=4):
 
 
 @pytest.mark.parametrize("n,qoi", [(4, api.QOI_AVG_DISP), (4, api.QOI_KS_VM),
-                                   # the survey's config 1 as specified: 10^3 cube, neo-Hookean,
-                                   # traction (10, 0, 0) on x=1, avg disp, nested mesh of 48,000 tets
+                                   # the small published-size case: 10^3 cube, neo-Hookean, traction
+                                   # (10, 0, 0) on x=1, avg disp, nested mesh of 48,000 tets
                                    (10, api.QOI_AVG_DISP)])
 def test_nested_adjoint_matches_oracle(n, qoi):
     mesh, mat, dbcs, tbcs = _primal_problem(n)
