@@ -653,6 +653,9 @@ def main():
     else:
         hbm_peak, peak_src = 6800.0, "fallback"
     alg = algorithmic_bytes(mesh.num_nodes, E, d.nnz)
+    peak_c = ctypes.c_double()
+    L.goal_measure_fp64_peak(ctypes.byref(peak_c))
+    fp64_peak = peak_c.value if peak_c.value > 0 else FP64_PEAK_TFLOPS
     # the dominant kernel is the element kernel (phase 1); its duration comes
     # from CUDA events on the assembly stream around its launch
     achieved = alg / (elem_ms * 1e-3) / 1e9
@@ -664,10 +667,11 @@ def main():
             pr = json.load(f)
         traffic = pr["dram_bytes_per_element"] * E
         flops = pr["fp64_flop_per_element"] * E
-        fp64 = {"achieved": flops / (elem_ms * 1e-3) / 1e12, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                "frac": flops / (elem_ms * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
+        fp64 = {"achieved": flops / (elem_ms * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": flops / (elem_ms * 1e-3) / 1e12 / fp64_peak,
                 "flop_per_element": pr["fp64_flop_per_element"],
-                "peak_source": "nominal: 2 DFMA/clk/SM x 152 SMs x 2070 MHz (no FP64 figure is measured)"}
+                "peak_source": "measured in this run: independent DFMA chains on every SM (goal_measure_fp64_peak)",
+                "nominal_peak": FP64_PEAK_TFLOPS}
     line = {
         "metric": METRIC, "value": value, "unit": "elem/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",

@@ -194,6 +194,11 @@ int goal_assemble(goal_mechanics m, goal_sol_info s, const goal_chain* chain, do
  * gathers of R, dMdu and the matrix blocks; count = assemblies measured. */
 int goal_assembly_timing(int enable);
 int goal_assembly_timing_read(double* ms, long long* count);
+/* No counterpart in the reference. Measured FP64 fused-multiply-add rate of
+ * the current GPU in TFLOP/s (eight independent chains per thread, best of
+ * five timed launches): the denominator of the element assembly's FP64
+ * roofline. */
+int goal_measure_fp64_peak(double* tflops);
 
 /* ---------------------------------------------------------------- boundary conditions
  * "dirichlet bcs: [eq, node set, expr]" and "traction bcs: [side set, Tx, Ty, Tz]". */

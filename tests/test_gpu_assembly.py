@@ -322,3 +322,13 @@ def test_single_element_and_single_colour():
         assert len(vals) == 256
         assert rel_vec(s.R, R) < RTOL
         assert rel_rows(s.dRdu_csr(), vals, g[0]) < RTOL
+
+
+def test_measured_fp64_peak_is_plausible():
+    """The FP64 roofline's denominator: GB300 issues 2 FP64 FMAs per clock per
+    SM (1.26 TFLOP/s at 2.07 GHz on 152 SMs)."""
+    import ctypes
+    from goal_gb300 import lib
+    v = ctypes.c_double()
+    assert lib().goal_measure_fp64_peak(ctypes.byref(v)) == 0
+    assert 0.5 < v.value < 2.0, v.value
