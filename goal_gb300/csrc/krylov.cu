@@ -68,6 +68,25 @@ __device__ __forceinline__ void load_row<float, __half>(const __half* p, float& 
   a = f0.x; b = f0.y; c = f1.x; d = f1.y;
 }
 
+// Basis entries in their storage type (the inner solve keeps its basis in
+// binary16), read and written in the arithmetic type.
+template <typename T, typename TV>
+__device__ __forceinline__ T ldv(const TV* p) {
+  return (T)(*p);
+}
+template <>
+__device__ __forceinline__ float ldv<float, __half>(const __half* p) {
+  return __half2float(*p);
+}
+template <typename TV, typename T>
+__device__ __forceinline__ void stv(TV* p, T v) {
+  *p = (TV)v;
+}
+template <>
+__device__ __forceinline__ void stv<__half, float>(__half* p, float v) {
+  *p = __float2half_rn(v);
+}
+
 // Block-row product of node n, row r: sum_k A_k[r,:] . x_{bcol[k]}, one fused
 // multiply-add per matrix entry (on GB300 the FP64 pipe, not HBM, bounds the
 // FP64 kernels, so no operation is spent on reductions).
@@ -121,16 +140,16 @@ __global__ void k_bj_col(int N, const T* __restrict__ Dinv, const T* V, T* Z, lo
 }
 
 // out = Dinv v_j with v_j = column j of V
-template <typename T>
-__global__ void k_bj_colin(int N, const T* __restrict__ Dinv, const T* V, long long ld, const GState* st,
+template <typename T, typename TV>
+__global__ void k_bj_colin(int N, const T* __restrict__ Dinv, const TV* V, long long ld, const GState* st,
                            T* __restrict__ out) {
   if (st->done) return;
-  const T* v = V + (long long)st->j * ld;
+  const TV* v = V + (long long)st->j * ld;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
     int n = i >> 2, r = i & 3;
     T d0, d1, d2, d3, x0, x1, x2, x3;
     Vec4<T>::load(Dinv + 16ll * n + 4 * r, d0, d1, d2, d3);
-    Vec4<T>::load(v + 4ll * n, x0, x1, x2, x3);
+    load_row<T, TV>(v + 4ll * n, x0, x1, x2, x3);
     out[i] = d0 * x0 + d1 * x1 + d2 * x2 + d3 * x3;
   }
 }
@@ -149,18 +168,18 @@ __global__ void k_bj(int N, const T* __restrict__ Dinv, const T* __restrict__ v,
 // Second, weighted block-Jacobi sweep of the learned preconditioner:
 // z += B (v - w) with w = A z, for column j of V and Z (state st; offset 0
 // and no gate without a state).
-template <typename T>
-__global__ void k_second_sweep_col(int N, const T* __restrict__ B, const T* V, long long ldv, const T* __restrict__ w,
+template <typename T, typename TV>
+__global__ void k_second_sweep_col(int N, const T* __restrict__ B, const TV* V, long long ldv, const T* __restrict__ w,
                                    T* Z, long long ldz, const GState* st) {
   if (st && st->done) return;
   const long long j = st ? st->j : 0;
-  const T* v = V + j * ldv;
+  const TV* v = V + j * ldv;
   T* z = Z + j * ldz;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * N; i += gridDim.x * blockDim.x) {
     int n = i >> 2, r = i & 3;
     T b0, b1, b2, b3, v0, v1, v2, v3, w0, w1, w2, w3;
     Vec4<T>::load(B + 16ll * n + 4 * r, b0, b1, b2, b3);
-    Vec4<T>::load(v + 4ll * n, v0, v1, v2, v3);
+    load_row<T, TV>(v + 4ll * n, v0, v1, v2, v3);
     Vec4<T>::load(w + 4ll * n, w0, w1, w2, w3);
     z[i] += b0 * (v0 - w0) + b1 * (v1 - w1) + b2 * (v2 - w2) + b3 * (v3 - w3);
   }
@@ -202,8 +221,8 @@ __device__ __forceinline__ T chunk_reduce(const T (&acc)[kDotChunk], T (*sm)[257
 
 // partial dot products of w with columns 0..j of V and with itself (column
 // j+1); part[c * gridDim.x + block]
-template <typename T, int R>
-__global__ void __launch_bounds__(256) k_multidot(long long n, const T* V, long long ld, const T* __restrict__ w,
+template <typename T, typename TV, int R>
+__global__ void __launch_bounds__(256) k_multidot(long long n, const TV* V, long long ld, const T* __restrict__ w,
                                                   const GState* st, double* part, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
@@ -225,11 +244,11 @@ __global__ void __launch_bounds__(256) k_multidot(long long n, const T* V, long 
       const int c = c0 + cc;
       T a = T(0);
       if (c <= j) {
-        const T* v = V + (long long)c * ld;
+        const TV* v = V + (long long)c * ld;
 #pragma unroll
         for (int q = 0; q < R; ++q) {
           const long long i = base + 256ll * q;
-          if (i < n) a = fma(v[i], wr[q], a);
+          if (i < n) a = fma(ldv<T, TV>(v + i), wr[q], a);
         }
       } else if (c == j + 1) {
 #pragma unroll
@@ -269,8 +288,8 @@ __global__ void k_dots_fin(int nbx, const double* part, GState* st, double* H, i
 }
 
 // w -= V dots ; partial |w|^2 per block
-template <typename T, int R>
-__global__ void __launch_bounds__(256) k_update(long long n, const T* V, long long ld, T* w, const double* dots,
+template <typename T, typename TV, int R>
+__global__ void __launch_bounds__(256) k_update(long long n, const TV* V, long long ld, T* w, const double* dots,
                                                 const GState* st, double* part, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
@@ -288,21 +307,21 @@ __global__ void __launch_bounds__(256) k_update(long long n, const T* V, long lo
   int c = 0;
   for (; c + 1 <= j; c += 2) {
     const T d0 = -sd[c], d1 = -sd[c + 1];
-    const T* v0 = V + (long long)c * ld;
-    const T* v1 = v0 + ld;
+    const TV* v0 = V + (long long)c * ld;
+    const TV* v1 = v0 + ld;
 #pragma unroll
     for (int q = 0; q < R; ++q) {
       const long long i = base + 256ll * q;
-      if (i < n) wr[q] = fma(d1, v1[i], fma(d0, v0[i], wr[q]));
+      if (i < n) wr[q] = fma(d1, ldv<T, TV>(v1 + i), fma(d0, ldv<T, TV>(v0 + i), wr[q]));
     }
   }
   for (; c <= j; ++c) {
     const T d0 = -sd[c];
-    const T* v0 = V + (long long)c * ld;
+    const TV* v0 = V + (long long)c * ld;
 #pragma unroll
     for (int q = 0; q < R; ++q) {
       const long long i = base + 256ll * q;
-      if (i < n) wr[q] = fma(d0, v0[i], wr[q]);
+      if (i < n) wr[q] = fma(d0, ldv<T, TV>(v0 + i), wr[q]);
     }
   }
   T acc = T(0);
@@ -359,20 +378,30 @@ struct Vec4Store<float> {
     *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
   }
 };
+template <>
+struct Vec4Store<__half> {
+  static __device__ __forceinline__ void store(__half* p, float a, float b, float c, float d) {
+    const __half2 h0 = __floats2half2_rn(a, b), h1 = __floats2half2_rn(c, d);
+    uint2 u;
+    u.x = *reinterpret_cast<const unsigned*>(&h0);
+    u.y = *reinterpret_cast<const unsigned*>(&h1);
+    *reinterpret_cast<uint2*>(p) = u;
+  }
+};
 
 // V_{j+1} = w / H[j+1, j], four entries per thread (n = 4 x nodes; every
 // column starts on a 32-byte boundary)
-template <typename T>
-__global__ void k_normalize(long long n, T* V, long long ld, const T* w, const GState* st, const double* H, int ldh) {
+template <typename T, typename TV>
+__global__ void k_normalize(long long n, TV* V, long long ld, const T* w, const GState* st, const double* H, int ldh) {
   if (st->done) return;
   const int j = st->j;
   const double h = H[j + 1 + (long long)ldh * j];
   const T inv = (h > 0.0) ? (T)(1.0 / h) : T(0);
-  T* v = V + (long long)(j + 1) * ld;
+  TV* v = V + (long long)(j + 1) * ld;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; 4 * q < n; q += (long long)gridDim.x * blockDim.x) {
     T a, b, c, d;
     Vec4<T>::load(w + 4 * q, a, b, c, d);
-    Vec4Store<T>::store(v + 4 * q, a * inv, b * inv, c * inv, d * inv);
+    Vec4Store<TV>::store(v + 4 * q, a * inv, b * inv, c * inv, d * inv);
   }
 }
 
@@ -465,16 +494,16 @@ __global__ void k_norm_givens(int nbx, const double* part, GState* st, double* H
 }
 
 // V_j = w / hnext after k_norm_givens advanced j
-template <typename T>
-__global__ void k_normalize_next(long long n, T* V, long long ld, const T* w, const GState* st) {
+template <typename T, typename TV>
+__global__ void k_normalize_next(long long n, TV* V, long long ld, const T* w, const GState* st) {
   if (st->done) return;
   const double h = st->hnext;
   const T inv = (h > 0.0) ? (T)(1.0 / h) : T(0);
-  T* v = V + (long long)st->j * ld;
+  TV* v = V + (long long)st->j * ld;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; 4 * q < n; q += (long long)gridDim.x * blockDim.x) {
     T a, b, c, d;
     Vec4<T>::load(w + 4 * q, a, b, c, d);
-    Vec4Store<T>::store(v + 4 * q, a * inv, b * inv, c * inv, d * inv);
+    Vec4Store<TV>::store(v + 4 * q, a * inv, b * inv, c * inv, d * inv);
   }
 }
 
@@ -545,9 +574,9 @@ __global__ void k_cycle_fin(int nbx, const double* part, GState* st, double* g, 
 template <typename T, typename TR>
 __global__ void k_scale_into(long long n, const TR* r, const GState* st, T* v0) {
   const double beta = st->beta;
-  const T inv = (T)(beta > 0.0 ? 1.0 / beta : 0.0);
+  const TR inv = (TR)(beta > 0.0 ? 1.0 / beta : 0.0);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    v0[i] = (T)r[i] * inv;
+    stv<T, TR>(v0 + i, r[i] * inv);
 }
 
 // The inner solve works in the dof-scaled space: r^ = S r in, z = S z^ out.
@@ -706,7 +735,7 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
   need(flag, 8);
   need(dots, kMaxM + 2);
   if (mixed) {
-    need(V32, nn * (mi_ + 1));
+    need(V16, nn * (mi_ + 1));
     need(w32, nn);
     need(r32, nn);
     need(t32, nn);
@@ -756,18 +785,18 @@ namespace {
 
 // Classical Gram-Schmidt of w against V_0..V_j, with a second pass when the
 // first one removed more than half of |w|^2 (device-side decision).
-template <typename T, int R>
-void orth_passes(long long n, T* V, T* w, GState* st, double* H, int ldh, double* dots, double* red, int jmax,
+template <typename T, typename TV, int R>
+void orth_passes(long long n, TV* V, T* w, GState* st, double* H, int ldh, double* dots, double* red, int jmax,
                  int passes, cudaStream_t s) {
   const int nbx = slab_grid(n, R);
   double* part = red;
   double* npart = red + (size_t)(kMaxM + 2) * nbx;
   for (int pass = 0; pass < passes; ++pass) {
-    k_multidot<T, R><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
+    k_multidot<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
     GOAL_CHECK_LAUNCH();
     k_dots_fin<<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
     GOAL_CHECK_LAUNCH();
-    k_update<T, R><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
+    k_update<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
     GOAL_CHECK_LAUNCH();
     if (passes > 1) {
       k_norm_fin<<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
@@ -778,17 +807,17 @@ void orth_passes(long long n, T* V, T* w, GState* st, double* H, int ldh, double
 
 // One Arnoldi step's orthogonalization (CGS with a conditional second pass),
 // normalization and Givens update, on state st.
-template <typename T>
-void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, double* cs, double* sn, double* g,
+template <typename T, typename TV>
+void arnoldi_orth(long long n, TV* V, T* w, GState* st, double* H, int ldh, double* cs, double* sn, double* g,
                   double* dots, double* red, int jmax, double tol_abs, int passes, cudaStream_t s) {
   switch (slab_rows<T>(n)) {
-    case 1: orth_passes<T, 1>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
-    case 2: orth_passes<T, 2>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
-    case 4: orth_passes<T, 4>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
-    default: orth_passes<T, 8>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
+    case 1: orth_passes<T, TV, 1>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
+    case 2: orth_passes<T, TV, 2>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
+    case 4: orth_passes<T, TV, 4>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
+    default: orth_passes<T, TV, 8>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
   }
   if (passes > 1) {
-    k_normalize<T><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st, H, ldh);
+    k_normalize<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st, H, ldh);
     GOAL_CHECK_LAUNCH();
     k_givens<<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
     GOAL_CHECK_LAUNCH();
@@ -797,7 +826,7 @@ void arnoldi_orth(long long n, T* V, T* w, GState* st, double* H, int ldh, doubl
     const int nbx = slab_grid(n, slab_rows<T>(n));
     k_norm_givens<<<1, 256, 0, s>>>(nbx, red + (size_t)(kMaxM + 2) * nbx, st, H, ldh, cs, sn, g, jmax, tol_abs);
     GOAL_CHECK_LAUNCH();
-    k_normalize_next<T><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st);
+    k_normalize_next<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st);
     GOAL_CHECK_LAUNCH();
   }
 }
@@ -902,13 +931,13 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       if (sweep2) {
         k_spmv_col<double, double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
         GOAL_CHECK_LAUNCH();
-        k_second_sweep_col<double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc.ptr, K.V.ptr, n, K.w.ptr, K.Z.ptr, n, st);
+        k_second_sweep_col<double, double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc.ptr, K.V.ptr, n, K.w.ptr, K.Z.ptr, n, st);
         GOAL_CHECK_LAUNCH();
       }
     } else {
       // inner GMRES in the dof-scaled space (FP32 vectors, A^ = S A S in
       // binary16) with the right preconditioner, fixed mi iterations:
-      // Z_j = S M^-1 V32 y with V32 the inner basis started from S V_j
+      // Z_j = S M^-1 V16 y with V16 the inner basis (binary16) started from S V_j
       k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.sd.ptr, K.r32.ptr);
       GOAL_CHECK_LAUNCH();
       k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.red.ptr);
@@ -917,29 +946,29 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       GOAL_CHECK_LAUNCH();
       k_gate<<<1, 1, 0, s>>>(st, sti);
       GOAL_CHECK_LAUNCH();
-      k_scale_into<float, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V32.ptr);
+      k_scale_into<__half, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V16.ptr);
       GOAL_CHECK_LAUNCH();
       for (int it = 0; it < mi; ++it) {
         // r32 = M^-1 v_it ; w32 = A^ r32 (ld 0 keeps the input at r32)
-        k_bj_colin<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V32.ptr, n, sti, K.r32.ptr);
+        k_bj_colin<float, __half><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V16.ptr, n, sti, K.r32.ptr);
         GOAL_CHECK_LAUNCH();
         if (sweep2) {
           k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
                                                          K.t32.ptr);
           GOAL_CHECK_LAUNCH();
-          k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V32.ptr, n, K.t32.ptr,
+          k_second_sweep_col<float, __half><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V16.ptr, n, K.t32.ptr,
                                                                      K.r32.ptr, 0, sti);
           GOAL_CHECK_LAUNCH();
         }
         k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
                                                        K.w32.ptr);
         GOAL_CHECK_LAUNCH();
-        arnoldi_orth<float>(n, K.V32.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0,
+        arnoldi_orth<float, __half>(n, K.V16.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0,
                             kInnerPasses, s);
       }
       k_backsolve<<<1, 1, 0, s>>>(sti, Hin, mi + 1, gin, yin);
       GOAL_CHECK_LAUNCH();
-      k_combine<float, float><<<nbx, 256, 0, s>>>(n, K.V32.ptr, n, yin, sti, K.w32.ptr, 1);
+      k_combine<__half, float><<<nbx, 256, 0, s>>>(n, K.V16.ptr, n, yin, sti, K.w32.ptr, 1);
       GOAL_CHECK_LAUNCH();
       k_bj<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.w32.ptr, K.r32.ptr);
       GOAL_CHECK_LAUNCH();
@@ -947,7 +976,7 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
         k_spmv<float, __half, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, nullptr,
                                                                    K.t32.ptr);
         GOAL_CHECK_LAUNCH();
-        k_second_sweep_col<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.w32.ptr, 0, K.t32.ptr,
+        k_second_sweep_col<float, float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.w32.ptr, 0, K.t32.ptr,
                                                                    K.r32.ptr, 0, nullptr);
         GOAL_CHECK_LAUNCH();
       }
@@ -956,7 +985,7 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
     }
     k_spmv_col<double, double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
     GOAL_CHECK_LAUNCH();
-    arnoldi_orth<double>(n, K.V.ptr, K.w.ptr, st, K.H.ptr, m + 1, K.cs.ptr, K.sn.ptr, K.g.ptr, dots, K.red.ptr, m,
+    arnoldi_orth<double, double>(n, K.V.ptr, K.w.ptr, st, K.H.ptr, m + 1, K.cs.ptr, K.sn.ptr, K.g.ptr, dots, K.red.ptr, m,
                          tol_abs, kOuterPasses, s);
   };
   // one Arnoldi step as a CUDA graph, captured once per solve; its kernels are

@@ -58,7 +58,8 @@ struct Krylov {
   int n = 0, m = 0, mi = 0;
   DevBuf<double> V, Z, w, r, H, cs, sn, g, y, red, scal, dots;
   DevBuf<double> Hi, csi, sni, gi, yi;   // inner (FP32 solve) Hessenberg and rotations
-  DevBuf<float> V32, w32, r32, t32;
+  DevBuf<float> w32, r32, t32;
+  DevBuf<__half> V16;      // the inner solve's Krylov basis (binary16 storage, FP32 arithmetic)
   // mixed mode: the inner solve's matrix S A S in binary16, S = diag(|a_ii|^-1/2)
   DevBuf<__half> A16;
   DevBuf<double> sd;
