@@ -26,7 +26,36 @@ struct GState {
   double res;   // |g[j]| residual estimate
   double beta;  // initial residual norm of the cycle
   double hnext; // |w| after a single-pass orthogonalization (read by the normalization)
+  double inv;   // 1/|w| (or 1/beta) for the next normalization, 0 for a zero norm
+  float inv32;  // the same in FP32, for the FP32 solve
+  float pad2;
 };
+
+// On GB300 every FP64 instruction occupies the FP64 pipe for a whole warp
+// (two lanes per clock per SM), so per-thread FP64 scalar work is costly: the
+// reciprocals for the normalizations are formed once, by the thread that
+// computed the norm, and the FP32 solve keeps its Hessenberg matrix, rotations
+// and partial sums in FP32.
+__device__ __forceinline__ void set_inv(GState* st, double h) {
+  st->inv = h > 0.0 ? 1.0 / h : 0.0;
+  st->inv32 = (float)st->inv;
+}
+__device__ __forceinline__ void set_inv(GState* st, float h) {
+  st->inv32 = h > 0.0f ? 1.0f / h : 0.0f;
+  st->inv = (double)st->inv32;
+}
+template <typename T>
+__device__ __forceinline__ T state_inv(const GState* st);
+template <>
+__device__ __forceinline__ double state_inv<double>(const GState* st) {
+  return st->inv;
+}
+template <>
+__device__ __forceinline__ float state_inv<float>(const GState* st) {
+  return st->inv32;
+}
+__device__ __forceinline__ double c_hypot(double a, double b) { return hypot(a, b); }
+__device__ __forceinline__ float c_hypot(float a, float b) { return hypotf(a, b); }
 
 constexpr int kMaxM = 256;
 constexpr int kDotChunk = 8;
@@ -56,6 +85,33 @@ struct Vec4<float> {
 
 // One row of a 4x4 matrix block in the arithmetic type T: same-type loads, or
 // four binary16 values (the inner solve's matrix) widened to float.
+template <typename T>
+struct Vec4Store;
+template <>
+struct Vec4Store<double> {
+  static __device__ __forceinline__ void store(double* p, double a, double b, double c, double d) {
+    double4_32a v;
+    v.x = a; v.y = b; v.z = c; v.w = d;
+    *reinterpret_cast<double4_32a*>(p) = v;
+  }
+};
+template <>
+struct Vec4Store<float> {
+  static __device__ __forceinline__ void store(float* p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+  }
+};
+template <>
+struct Vec4Store<__half> {
+  static __device__ __forceinline__ void store(__half* p, float a, float b, float c, float d) {
+    const __half2 h0 = __floats2half2_rn(a, b), h1 = __floats2half2_rn(c, d);
+    uint2 u;
+    u.x = *reinterpret_cast<const unsigned*>(&h0);
+    u.y = *reinterpret_cast<const unsigned*>(&h1);
+    *reinterpret_cast<uint2*>(p) = u;
+  }
+};
+
 template <typename T, typename TA>
 __device__ __forceinline__ void load_row(const TA* p, T& a, T& b, T& c, T& d) {
   Vec4<T>::load(p, a, b, c, d);
@@ -223,7 +279,7 @@ __device__ __forceinline__ T chunk_reduce(const T (&acc)[kDotChunk], T (*sm)[257
 // j+1); part[c * gridDim.x + block]
 template <typename T, typename TV, int R>
 __global__ void __launch_bounds__(256) k_multidot(long long n, const TV* V, long long ld, const T* __restrict__ w,
-                                                  const GState* st, double* part, int pass) {
+                                                  const GState* st, T* part, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
   const int j = st->j;
@@ -258,24 +314,25 @@ __global__ void __launch_bounds__(256) k_multidot(long long n, const TV* V, long
     }
     const T v = chunk_reduce<T>(acc, sm);
     const int c = c0 + wid;
-    if (lane == 0 && c < ncols) part[(long long)c * gridDim.x + blockIdx.x] = (double)v;
+    if (lane == 0 && c < ncols) part[(long long)c * gridDim.x + blockIdx.x] = v;
   }
 }
 
-__global__ void k_dots_fin(int nbx, const double* part, GState* st, double* H, int ldh, double* dots, int pass) {
+template <typename C>
+__global__ void k_dots_fin(int nbx, const C* part, GState* st, C* H, int ldh, C* dots, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
   const int j = st->j;
   const int c = blockIdx.x;
   if (c > j + 1) return;
-  double v = 0.0;
+  C v = C(0);
   for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[(long long)c * nbx + k];
-  __shared__ double sm[32];
+  __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
+    C s = C(0);
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
     if (c <= j) {
       dots[c] = s;
@@ -289,8 +346,8 @@ __global__ void k_dots_fin(int nbx, const double* part, GState* st, double* H, i
 
 // w -= V dots ; partial |w|^2 per block
 template <typename T, typename TV, int R>
-__global__ void __launch_bounds__(256) k_update(long long n, const TV* V, long long ld, T* w, const double* dots,
-                                                const GState* st, double* part, int pass) {
+__global__ void __launch_bounds__(256) k_update(long long n, const TV* V, long long ld, T* w, const T* dots,
+                                                const GState* st, T* part, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
   const int j = st->j;
@@ -340,63 +397,148 @@ __global__ void __launch_bounds__(256) k_update(long long n, const TV* V, long l
   if (threadIdx.x == 0) {
     T s = T(0);
     for (int k = 0; k < 8; ++k) s += sm[k];
-    part[blockIdx.x] = (double)s;
+    part[blockIdx.x] = s;
   }
 }
 
-__global__ void k_norm_fin(int nbx, const double* part, GState* st, double* H, int ldh, int pass) {
+// Variants for a binary16 basis: every thread owns G groups of four
+// consecutive rows (n = 4 x nodes, so a group is all in or all out), reads a
+// group of w as one 16-byte load and a group of a basis column as one 8-byte
+// load; a block covers 1024 G rows. Same sums as k_multidot / k_update.
+template <typename T, typename TV, int G>
+__global__ void __launch_bounds__(256) k_multidot_v(long long n, const TV* V, long long ld, const T* __restrict__ w,
+                                                    const GState* st, T* part, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
-  double v = 0.0;
+  const int j = st->j;
+  const int ncols = j + 2;
+  const long long base = (long long)blockIdx.x * (1024ll * G) + 4 * threadIdx.x;
+  T wr[G][4];
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    const long long i = base + 1024ll * q;
+    if (i < n) Vec4<T>::load(w + i, wr[q][0], wr[q][1], wr[q][2], wr[q][3]);
+    else wr[q][0] = wr[q][1] = wr[q][2] = wr[q][3] = T(0);
+  }
+  __shared__ T sm[kDotChunk][257];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int c0 = 0; c0 < ncols; c0 += kDotChunk) {
+    T acc[kDotChunk];
+#pragma unroll
+    for (int cc = 0; cc < kDotChunk; ++cc) {
+      const int c = c0 + cc;
+      T a = T(0);
+      if (c <= j) {
+        const TV* v = V + (long long)c * ld;
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+          const long long i = base + 1024ll * q;
+          if (i < n) {
+            T x0, x1, x2, x3;
+            load_row<T, TV>(v + i, x0, x1, x2, x3);
+            a = fma(x0, wr[q][0], a);
+            a = fma(x1, wr[q][1], a);
+            a = fma(x2, wr[q][2], a);
+            a = fma(x3, wr[q][3], a);
+          }
+        }
+      } else if (c == j + 1) {
+#pragma unroll
+        for (int q = 0; q < G; ++q)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) a = fma(wr[q][e], wr[q][e], a);
+      }
+      acc[cc] = a;
+    }
+    const T v = chunk_reduce<T>(acc, sm);
+    const int c = c0 + wid;
+    if (lane == 0 && c < ncols) part[(long long)c * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+template <typename T, typename TV, int G>
+__global__ void __launch_bounds__(256) k_update_v(long long n, const TV* V, long long ld, T* w, const T* dots,
+                                                  const GState* st, T* part, int pass) {
+  if (st->done) return;
+  if (pass == 1 && !st->reorth) return;
+  const int j = st->j;
+  __shared__ T sd[kMaxM + 1];
+  for (int c = threadIdx.x; c <= j; c += blockDim.x) sd[c] = dots[c];
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * (1024ll * G) + 4 * threadIdx.x;
+  T wr[G][4];
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    const long long i = base + 1024ll * q;
+    if (i < n) Vec4<T>::load(w + i, wr[q][0], wr[q][1], wr[q][2], wr[q][3]);
+    else wr[q][0] = wr[q][1] = wr[q][2] = wr[q][3] = T(0);
+  }
+  for (int c = 0; c <= j; ++c) {
+    const T d = -sd[c];
+    const TV* v = V + (long long)c * ld;
+#pragma unroll
+    for (int q = 0; q < G; ++q) {
+      const long long i = base + 1024ll * q;
+      if (i < n) {
+        T x0, x1, x2, x3;
+        load_row<T, TV>(v + i, x0, x1, x2, x3);
+        wr[q][0] = fma(d, x0, wr[q][0]);
+        wr[q][1] = fma(d, x1, wr[q][1]);
+        wr[q][2] = fma(d, x2, wr[q][2]);
+        wr[q][3] = fma(d, x3, wr[q][3]);
+      }
+    }
+  }
+  T acc = T(0);
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    const long long i = base + 1024ll * q;
+    if (i < n) {
+      Vec4Store<T>::store(w + i, wr[q][0], wr[q][1], wr[q][2], wr[q][3]);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc = fma(wr[q][e], wr[q][e], acc);
+    }
+  }
+  __shared__ T sm[8];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T s = T(0);
+    for (int k = 0; k < 8; ++k) s += sm[k];
+    part[blockIdx.x] = s;
+  }
+}
+
+template <typename C>
+__global__ void k_norm_fin(int nbx, const C* part, GState* st, C* H, int ldh, int pass) {
+  if (st->done) return;
+  if (pass == 1 && !st->reorth) return;
+  C v = C(0);
   for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
-  __shared__ double sm[32];
+  __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
+    C s = C(0);
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
     const int j = st->j;
-    if (pass == 0) st->reorth = (s < 0.5 * st->wb2) ? 1 : 0;
-    H[j + 1 + (long long)ldh * j] = sqrt(s);
+    if (pass == 0) st->reorth = (s < C(0.5) * (C)st->wb2) ? 1 : 0;
+    const C h = sqrt(s);
+    H[j + 1 + (long long)ldh * j] = h;
+    set_inv(st, h);
   }
 }
 
-template <typename T>
-struct Vec4Store;
-template <>
-struct Vec4Store<double> {
-  static __device__ __forceinline__ void store(double* p, double a, double b, double c, double d) {
-    double4_32a v;
-    v.x = a; v.y = b; v.z = c; v.w = d;
-    *reinterpret_cast<double4_32a*>(p) = v;
-  }
-};
-template <>
-struct Vec4Store<float> {
-  static __device__ __forceinline__ void store(float* p, float a, float b, float c, float d) {
-    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
-  }
-};
-template <>
-struct Vec4Store<__half> {
-  static __device__ __forceinline__ void store(__half* p, float a, float b, float c, float d) {
-    const __half2 h0 = __floats2half2_rn(a, b), h1 = __floats2half2_rn(c, d);
-    uint2 u;
-    u.x = *reinterpret_cast<const unsigned*>(&h0);
-    u.y = *reinterpret_cast<const unsigned*>(&h1);
-    *reinterpret_cast<uint2*>(p) = u;
-  }
-};
 
 // V_{j+1} = w / H[j+1, j], four entries per thread (n = 4 x nodes; every
 // column starts on a 32-byte boundary)
 template <typename T, typename TV>
-__global__ void k_normalize(long long n, TV* V, long long ld, const T* w, const GState* st, const double* H, int ldh) {
+__global__ void k_normalize(long long n, TV* V, long long ld, const T* w, const GState* st) {
   if (st->done) return;
   const int j = st->j;
-  const double h = H[j + 1 + (long long)ldh * j];
-  const T inv = (h > 0.0) ? (T)(1.0 / h) : T(0);
+  const T inv = state_inv<T>(st);
   TV* v = V + (long long)(j + 1) * ld;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; 4 * q < n; q += (long long)gridDim.x * blockDim.x) {
     T a, b, c, d;
@@ -407,11 +549,12 @@ __global__ void k_normalize(long long n, TV* V, long long ld, const T* w, const 
 
 // Applies the previous rotations to the new Hessenberg column (staged in
 // shared memory by the whole block), then forms rotation j (thread 0).
-__global__ void k_givens(GState* st, double* H, int ldh, double* cs, double* sn, double* g, int jmax, double tol_abs) {
+template <typename C>
+__global__ void k_givens(GState* st, C* H, int ldh, C* cs, C* sn, C* g, int jmax, double tol_abs) {
   if (st->done) return;
   const int j = st->j;
-  double* h = H + (long long)ldh * j;
-  __shared__ double sh[kMaxM + 2], scs[kMaxM + 1], ssn[kMaxM + 1];
+  C* h = H + (long long)ldh * j;
+  __shared__ C sh[kMaxM + 2], scs[kMaxM + 1], ssn[kMaxM + 1];
   for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) sh[i] = h[i];
   for (int i = threadIdx.x; i < j; i += blockDim.x) {
     scs[i] = cs[i];
@@ -420,23 +563,23 @@ __global__ void k_givens(GState* st, double* H, int ldh, double* cs, double* sn,
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int i = 0; i < j; ++i) {
-      const double t = scs[i] * sh[i] + ssn[i] * sh[i + 1];
+      const C t = scs[i] * sh[i] + ssn[i] * sh[i + 1];
       sh[i + 1] = -ssn[i] * sh[i] + scs[i] * sh[i + 1];
       sh[i] = t;
     }
-    const double a = sh[j], b = sh[j + 1];
-    const double r = hypot(a, b);
-    double c = 1.0, s = 0.0;
-    if (r > 0.0) { c = a / r; s = b / r; }
+    const C a = sh[j], b = sh[j + 1];
+    const C r = c_hypot(a, b);
+    C c = C(1), s = C(0);
+    if (r > C(0)) { c = a / r; s = b / r; }
     cs[j] = c;
     sn[j] = s;
     sh[j] = r;
-    sh[j + 1] = 0.0;
+    sh[j + 1] = C(0);
     g[j + 1] = -s * g[j];
     g[j] = c * g[j];
-    st->res = fabs(g[j + 1]);
+    st->res = (double)fabs(g[j + 1]);
     st->j = j + 1;
-    if (st->res <= tol_abs || st->j >= jmax || b == 0.0 || !(st->res == st->res)) st->done = 1;
+    if (st->res <= tol_abs || st->j >= jmax || b == C(0) || !(st->res == st->res)) st->done = 1;
   }
   __syncthreads();
   for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) h[i] = sh[i];
@@ -444,23 +587,25 @@ __global__ void k_givens(GState* st, double* H, int ldh, double* cs, double* sn,
 
 // Single-pass orthogonalization: |w| from the block partials (H[j+1, j] and
 // hnext), then the Givens step, in one block.
-__global__ void k_norm_givens(int nbx, const double* part, GState* st, double* H, int ldh, double* cs, double* sn,
-                              double* g, int jmax, double tol_abs) {
+template <typename C>
+__global__ void k_norm_givens(int nbx, const C* part, GState* st, C* H, int ldh, C* cs, C* sn, C* g, int jmax,
+                              double tol_abs) {
   if (st->done) return;
   const int j = st->j;
-  double v = 0.0;
+  C v = C(0);
   for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
-  __shared__ double sm[32];
+  __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
   __syncthreads();
-  double* h = H + (long long)ldh * j;
-  __shared__ double sh[kMaxM + 2], scs[kMaxM + 1], ssn[kMaxM + 1];
+  C* h = H + (long long)ldh * j;
+  __shared__ C sh[kMaxM + 2], scs[kMaxM + 1], ssn[kMaxM + 1];
   if (threadIdx.x == 0) {
-    double s2 = 0.0;
+    C s2 = C(0);
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s2 += sm[k];
-    const double nrm = sqrt(s2);
-    st->hnext = nrm;
+    const C nrm = sqrt(s2);
+    st->hnext = (double)nrm;
+    set_inv(st, nrm);
     sh[j + 1] = nrm;
   }
   for (int i = threadIdx.x; i <= j; i += blockDim.x) sh[i] = h[i];
@@ -471,23 +616,23 @@ __global__ void k_norm_givens(int nbx, const double* part, GState* st, double* H
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int i = 0; i < j; ++i) {
-      const double t = scs[i] * sh[i] + ssn[i] * sh[i + 1];
+      const C t = scs[i] * sh[i] + ssn[i] * sh[i + 1];
       sh[i + 1] = -ssn[i] * sh[i] + scs[i] * sh[i + 1];
       sh[i] = t;
     }
-    const double a = sh[j], b = sh[j + 1];
-    const double r = hypot(a, b);
-    double c = 1.0, s = 0.0;
-    if (r > 0.0) { c = a / r; s = b / r; }
+    const C a = sh[j], b = sh[j + 1];
+    const C r = c_hypot(a, b);
+    C c = C(1), s = C(0);
+    if (r > C(0)) { c = a / r; s = b / r; }
     cs[j] = c;
     sn[j] = s;
     sh[j] = r;
-    sh[j + 1] = 0.0;
+    sh[j + 1] = C(0);
     g[j + 1] = -s * g[j];
     g[j] = c * g[j];
-    st->res = fabs(g[j + 1]);
+    st->res = (double)fabs(g[j + 1]);
     st->j = j + 1;
-    if (st->res <= tol_abs || st->j >= jmax || b == 0.0 || !(st->res == st->res)) st->done = 1;
+    if (st->res <= tol_abs || st->j >= jmax || b == C(0) || !(st->res == st->res)) st->done = 1;
   }
   __syncthreads();
   for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) h[i] = sh[i];
@@ -497,8 +642,7 @@ __global__ void k_norm_givens(int nbx, const double* part, GState* st, double* H
 template <typename T, typename TV>
 __global__ void k_normalize_next(long long n, TV* V, long long ld, const T* w, const GState* st) {
   if (st->done) return;
-  const double h = st->hnext;
-  const T inv = (h > 0.0) ? (T)(1.0 / h) : T(0);
+  const T inv = state_inv<T>(st);
   TV* v = V + (long long)st->j * ld;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; 4 * q < n; q += (long long)gridDim.x * blockDim.x) {
     T a, b, c, d;
@@ -507,33 +651,46 @@ __global__ void k_normalize_next(long long n, TV* V, long long ld, const T* w, c
   }
 }
 
-__global__ void k_backsolve(const GState* st, const double* H, int ldh, const double* g, double* y) {
+// y = R^-1 g for the k x k upper triangle R of the rotated Hessenberg matrix,
+// one warp: reciprocals of the diagonal first (in parallel), then column by
+// column, y_i = s_i / R_ii and s_r -= R_ri y_i for r < i across the lanes.
+template <typename C>
+__global__ void k_backsolve(const GState* st, const C* H, int ldh, const C* g, C* y) {
   const int k = st->j;
+  const int lane = threadIdx.x;
+  __shared__ C s[kMaxM + 1], dinv[kMaxM + 1];
+  for (int r = lane; r < k; r += 32) {
+    const C d = H[r + (long long)ldh * r];
+    dinv[r] = d != C(0) ? C(1) / d : C(0);
+    s[r] = g[r];
+  }
+  __syncwarp();
   for (int i = k - 1; i >= 0; --i) {
-    double s = g[i];
-    for (int c = i + 1; c < k; ++c) s -= H[i + (long long)ldh * c] * y[c];
-    const double d = H[i + (long long)ldh * i];
-    y[i] = (d != 0.0) ? s / d : 0.0;
+    const C yi = s[i] * dinv[i];
+    if (lane == 0) y[i] = yi;
+    const C* h = H + (long long)ldh * i;
+    for (int r = lane; r < i; r += 32) s[r] -= h[r] * yi;
+    __syncwarp();
   }
 }
 
+// x (+)= Z y; TX = float (the inner solve) works in FP32 throughout, with y
+// in FP32, TX = double in FP64.
 template <typename T, typename TX>
-__global__ void k_combine(long long n, const T* Z, long long ld, const double* y, const GState* st, TX* x, int zero_first) {
+__global__ void k_combine(long long n, const T* Z, long long ld, const TX* y, const GState* st, TX* x, int zero_first) {
   const int k = st->j;
-  __shared__ double sy[kMaxM];
+  __shared__ TX sy[kMaxM];
   for (int c = threadIdx.x; c < k; c += blockDim.x) sy[c] = y[c];
   __syncthreads();
-  // FP64 results accumulate in FP64; an FP32 result (the inner solve) in FP32
-  using Acc = typename std::conditional<std::is_same<TX, float>::value, float, double>::type;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    Acc s = zero_first ? Acc(0) : (Acc)x[i];
-    for (int c = 0; c < k; ++c) s = fma((Acc)sy[c], (Acc)Z[c * ld + i], s);
-    x[i] = (TX)s;
+    TX s = zero_first ? TX(0) : x[i];
+    for (int c = 0; c < k; ++c) s = fma(sy[c], ldv<TX, T>(Z + c * ld + i), s);
+    x[i] = s;
   }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_norm2_part(long long n, const T* x, double* part) {
+__global__ void __launch_bounds__(256) k_norm2_part(long long n, const T* x, T* part) {
   T a = T(0);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     a = fma(x[i], x[i], a);
@@ -544,37 +701,38 @@ __global__ void __launch_bounds__(256) k_norm2_part(long long n, const T* x, dou
   if (threadIdx.x == 0) {
     T s = T(0);
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
-    part[blockIdx.x] = (double)s;
+    part[blockIdx.x] = s;
   }
 }
 
 // beta = |r| from partials; V_0 = r / beta; g = [beta, 0, ...]; state reset
-__global__ void k_cycle_fin(int nbx, const double* part, GState* st, double* g, int m, double* out_beta) {
-  double v = 0.0;
+template <typename C>
+__global__ void k_cycle_fin(int nbx, const C* part, GState* st, C* g, int m, double* out_beta) {
+  C v = C(0);
   for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
-  __shared__ double sm[32];
+  __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
+    C s = C(0);
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
-    double beta = sqrt(s);
-    st->beta = beta;
+    const C beta = sqrt(s);
+    st->beta = (double)beta;
+    set_inv(st, beta);
     st->j = 0;
     st->reorth = 0;
-    st->res = beta;
-    st->done = (beta > 0.0 && beta == beta) ? 0 : 1;
+    st->res = (double)beta;
+    st->done = (beta > C(0) && beta == beta) ? 0 : 1;
     g[0] = beta;
-    for (int i = 1; i <= m; ++i) g[i] = 0.0;
-    if (out_beta) *out_beta = beta;
+    for (int i = 1; i <= m; ++i) g[i] = C(0);
+    if (out_beta) *out_beta = (double)beta;
   }
 }
 
 template <typename T, typename TR>
 __global__ void k_scale_into(long long n, const TR* r, const GState* st, T* v0) {
-  const double beta = st->beta;
-  const TR inv = (TR)(beta > 0.0 ? 1.0 / beta : 0.0);
+  const TR inv = state_inv<TR>(st);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     stv<T, TR>(v0 + i, r[i] * inv);
 }
@@ -710,6 +868,12 @@ int slab_rows(long long n) {
   return r;
 }
 int slab_grid(long long n, int rows) { return (int)std::max(1ll, (n + 256ll * rows - 1) / (256ll * rows)); }
+// a binary16 basis is read in groups of four rows: at least 4 rows per thread
+template <typename T, typename TV>
+int orth_rows(long long n) {
+  const int r = slab_rows<T>(n);
+  return std::is_same<TV, __half>::value ? std::max(r, 4) : r;
+}
 
 }  // namespace
 
@@ -786,20 +950,23 @@ namespace {
 // Classical Gram-Schmidt of w against V_0..V_j, with a second pass when the
 // first one removed more than half of |w|^2 (device-side decision).
 template <typename T, typename TV, int R>
-void orth_passes(long long n, TV* V, T* w, GState* st, double* H, int ldh, double* dots, double* red, int jmax,
-                 int passes, cudaStream_t s) {
+void orth_passes(long long n, TV* V, T* w, GState* st, T* H, int ldh, T* dots, T* red, int jmax, int passes,
+                 cudaStream_t s) {
   const int nbx = slab_grid(n, R);
-  double* part = red;
-  double* npart = red + (size_t)(kMaxM + 2) * nbx;
+  T* part = red;
+  T* npart = red + (size_t)(kMaxM + 2) * nbx;
+  constexpr bool vec = std::is_same<TV, __half>::value && R >= 4;
   for (int pass = 0; pass < passes; ++pass) {
-    k_multidot<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
+    if constexpr (vec) k_multidot_v<T, TV, R / 4><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
+    else k_multidot<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
     GOAL_CHECK_LAUNCH();
-    k_dots_fin<<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
+    k_dots_fin<T><<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
     GOAL_CHECK_LAUNCH();
-    k_update<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
+    if constexpr (vec) k_update_v<T, TV, R / 4><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
+    else k_update<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
     GOAL_CHECK_LAUNCH();
     if (passes > 1) {
-      k_norm_fin<<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
+      k_norm_fin<T><<<1, 256, 0, s>>>(nbx, npart, st, H, ldh, pass);
       GOAL_CHECK_LAUNCH();
     }
   }
@@ -808,23 +975,23 @@ void orth_passes(long long n, TV* V, T* w, GState* st, double* H, int ldh, doubl
 // One Arnoldi step's orthogonalization (CGS with a conditional second pass),
 // normalization and Givens update, on state st.
 template <typename T, typename TV>
-void arnoldi_orth(long long n, TV* V, T* w, GState* st, double* H, int ldh, double* cs, double* sn, double* g,
-                  double* dots, double* red, int jmax, double tol_abs, int passes, cudaStream_t s) {
-  switch (slab_rows<T>(n)) {
+void arnoldi_orth(long long n, TV* V, T* w, GState* st, T* H, int ldh, T* cs, T* sn, T* g, T* dots, T* red, int jmax,
+                  double tol_abs, int passes, cudaStream_t s) {
+  switch (orth_rows<T, TV>(n)) {
     case 1: orth_passes<T, TV, 1>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
     case 2: orth_passes<T, TV, 2>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
     case 4: orth_passes<T, TV, 4>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
     default: orth_passes<T, TV, 8>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
   }
   if (passes > 1) {
-    k_normalize<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st, H, ldh);
+    k_normalize<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st);
     GOAL_CHECK_LAUNCH();
-    k_givens<<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
+    k_givens<T><<<1, 128, 0, s>>>(st, H, ldh, cs, sn, g, jmax, tol_abs);
     GOAL_CHECK_LAUNCH();
   } else {
     // one pass: norm and Givens in one block, then V_{j+1} = w / |w|
-    const int nbx = slab_grid(n, slab_rows<T>(n));
-    k_norm_givens<<<1, 256, 0, s>>>(nbx, red + (size_t)(kMaxM + 2) * nbx, st, H, ldh, cs, sn, g, jmax, tol_abs);
+    const int nbx = slab_grid(n, orth_rows<T, TV>(n));
+    k_norm_givens<T><<<1, 256, 0, s>>>(nbx, red + (size_t)(kMaxM + 2) * nbx, st, H, ldh, cs, sn, g, jmax, tol_abs);
     GOAL_CHECK_LAUNCH();
     k_normalize_next<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st);
     GOAL_CHECK_LAUNCH();
@@ -835,8 +1002,8 @@ double read_norm(long long n, const double* x, Krylov& K) {
   const int nbx = vec_grid(n);
   k_norm2_part<double><<<nbx, 256, 0, K.stream>>>(n, x, K.red.ptr);
   GOAL_CHECK_LAUNCH();
-  k_cycle_fin<<<1, 256, 0, K.stream>>>(nbx, K.red.ptr, reinterpret_cast<GState*>(K.scal.ptr + 16), K.scal.ptr + 40,
-                                       0, K.scal.ptr + 8);
+  k_cycle_fin<double><<<1, 256, 0, K.stream>>>(nbx, K.red.ptr, reinterpret_cast<GState*>(K.scal.ptr + 16),
+                                               K.scal.ptr + 40, 0, K.scal.ptr + 8);
   GOAL_CHECK_LAUNCH();
   GOAL_CUDA(cudaMemcpyAsync(K.h_scal, K.scal.ptr + 8, sizeof(double), cudaMemcpyDeviceToHost, K.stream));
   GOAL_CUDA(cudaStreamSynchronize(K.stream));
@@ -903,11 +1070,15 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
   GState* st = reinterpret_cast<GState*>(K.scal.ptr);         // outer state
   GState* sti = reinterpret_cast<GState*>(K.scal.ptr + 24);   // inner state
   double* dots = K.dots.ptr;
-  double* Hin = mixed ? K.Hi.ptr : nullptr;
-  double* csin = mixed ? K.csi.ptr : nullptr;
-  double* snin = mixed ? K.sni.ptr : nullptr;
-  double* gin = mixed ? K.gi.ptr : nullptr;
-  double* yin = mixed ? K.yi.ptr : nullptr;
+  // the inner solve's Hessenberg matrix, rotations, partial sums and dot
+  // products are FP32 (in the FP64 buffers reserved for them)
+  float* Hin = mixed ? reinterpret_cast<float*>(K.Hi.ptr) : nullptr;
+  float* csin = mixed ? reinterpret_cast<float*>(K.csi.ptr) : nullptr;
+  float* snin = mixed ? reinterpret_cast<float*>(K.sni.ptr) : nullptr;
+  float* gin = mixed ? reinterpret_cast<float*>(K.gi.ptr) : nullptr;
+  float* yin = mixed ? reinterpret_cast<float*>(K.yi.ptr) : nullptr;
+  float* dots32 = reinterpret_cast<float*>(K.dots.ptr);
+  float* red32 = reinterpret_cast<float*>(K.red.ptr);
 
   const double bnorm = read_norm(n, b, K);
   const double tol_abs = p.tolerance * (bnorm > 0.0 ? bnorm : 1.0);
@@ -940,9 +1111,9 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       // Z_j = S M^-1 V16 y with V16 the inner basis (binary16) started from S V_j
       k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.sd.ptr, K.r32.ptr);
       GOAL_CHECK_LAUNCH();
-      k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.red.ptr);
+      k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, red32);
       GOAL_CHECK_LAUNCH();
-      k_cycle_fin<<<1, 256, 0, s>>>(nbx, K.red.ptr, sti, gin, mi, nullptr);
+      k_cycle_fin<float><<<1, 256, 0, s>>>(nbx, red32, sti, gin, mi, nullptr);
       GOAL_CHECK_LAUNCH();
       k_gate<<<1, 1, 0, s>>>(st, sti);
       GOAL_CHECK_LAUNCH();
@@ -963,10 +1134,10 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
         k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
                                                        K.w32.ptr);
         GOAL_CHECK_LAUNCH();
-        arnoldi_orth<float, __half>(n, K.V16.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots, K.red.ptr, mi, 0.0,
-                            kInnerPasses, s);
+        arnoldi_orth<float, __half>(n, K.V16.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots32, red32, mi, 0.0,
+                                    kInnerPasses, s);
       }
-      k_backsolve<<<1, 1, 0, s>>>(sti, Hin, mi + 1, gin, yin);
+      k_backsolve<float><<<1, 32, 0, s>>>(sti, Hin, mi + 1, gin, yin);
       GOAL_CHECK_LAUNCH();
       k_combine<__half, float><<<nbx, 256, 0, s>>>(n, K.V16.ptr, n, yin, sti, K.w32.ptr, 1);
       GOAL_CHECK_LAUNCH();
@@ -998,7 +1169,7 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
     // start a cycle: V_0 = r / beta
     k_norm2_part<double><<<nbx, 256, 0, s>>>(n, K.r.ptr, K.red.ptr);
     GOAL_CHECK_LAUNCH();
-    k_cycle_fin<<<1, 256, 0, s>>>(nbx, K.red.ptr, st, K.g.ptr, m, nullptr);
+    k_cycle_fin<double><<<1, 256, 0, s>>>(nbx, K.red.ptr, st, K.g.ptr, m, nullptr);
     GOAL_CHECK_LAUNCH();
     k_scale_into<double, double><<<nbx, 256, 0, s>>>(n, K.r.ptr, st, K.V.ptr);
     GOAL_CHECK_LAUNCH();
@@ -1024,7 +1195,7 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       out.spmv64 += (long long)done_steps * (1 + extra);
     }
     out.iters += done_steps;
-    k_backsolve<<<1, 1, 0, s>>>(st, K.H.ptr, m + 1, K.g.ptr, K.y.ptr);
+    k_backsolve<double><<<1, 32, 0, s>>>(st, K.H.ptr, m + 1, K.g.ptr, K.y.ptr);
     GOAL_CHECK_LAUNCH();
     k_combine<double, double><<<nbx, 256, 0, s>>>(n, K.Z.ptr, n, K.y.ptr, st, x, 0);
     GOAL_CHECK_LAUNCH();
