@@ -55,6 +55,24 @@ __device__ __forceinline__ float state_inv<float>(const GState* st) {
   return st->inv32;
 }
 __device__ __forceinline__ double c_hypot(double a, double b) { return hypot(a, b); }
+
+// This thread's share of a sum of n block partials (stride blockDim.x), four
+// independent loads in flight: the sum of a few thousand partials is bound
+// by memory latency, not by the adds.
+template <typename C>
+__device__ __forceinline__ C thread_partial_sum(const C* __restrict__ p, int n) {
+  const int nt = blockDim.x;
+  C a0 = C(0), a1 = C(0), a2 = C(0), a3 = C(0);
+  int k = threadIdx.x;
+  for (; k + 3 * nt < n; k += 4 * nt) {
+    a0 += p[k];
+    a1 += p[k + nt];
+    a2 += p[k + 2 * nt];
+    a3 += p[k + 3 * nt];
+  }
+  for (; k < n; k += nt) a0 += p[k];
+  return (a0 + a1) + (a2 + a3);
+}
 __device__ __forceinline__ float c_hypot(float a, float b) { return hypotf(a, b); }
 
 constexpr int kMaxM = 256;
@@ -325,8 +343,7 @@ __global__ void k_dots_fin(int nbx, const C* part, GState* st, C* H, int ldh, C*
   const int j = st->j;
   const int c = blockIdx.x;
   if (c > j + 1) return;
-  C v = C(0);
-  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[(long long)c * nbx + k];
+  C v = thread_partial_sum<C>(part + (long long)c * nbx, nbx);
   __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
@@ -514,8 +531,7 @@ template <typename C>
 __global__ void k_norm_fin(int nbx, const C* part, GState* st, C* H, int ldh, int pass) {
   if (st->done) return;
   if (pass == 1 && !st->reorth) return;
-  C v = C(0);
-  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
+  C v = thread_partial_sum<C>(part, nbx);
   __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
@@ -592,8 +608,7 @@ __global__ void k_norm_givens(int nbx, const C* part, GState* st, C* H, int ldh,
                               double tol_abs) {
   if (st->done) return;
   const int j = st->j;
-  C v = C(0);
-  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
+  C v = thread_partial_sum<C>(part, nbx);
   __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
@@ -708,8 +723,7 @@ __global__ void __launch_bounds__(256) k_norm2_part(long long n, const T* x, T* 
 // beta = |r| from partials; V_0 = r / beta; g = [beta, 0, ...]; state reset
 template <typename C>
 __global__ void k_cycle_fin(int nbx, const C* part, GState* st, C* g, int m, double* out_beta) {
-  C v = C(0);
-  for (int k = threadIdx.x; k < nbx; k += blockDim.x) v += part[k];
+  C v = thread_partial_sum<C>(part, nbx);
   __shared__ C sm[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
@@ -960,7 +974,7 @@ void orth_passes(long long n, TV* V, T* w, GState* st, T* H, int ldh, T* dots, T
     if constexpr (vec) k_multidot_v<T, TV, R / 4><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
     else k_multidot<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, st, part, pass);
     GOAL_CHECK_LAUNCH();
-    k_dots_fin<T><<<jmax + 2, 128, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
+    k_dots_fin<T><<<jmax + 2, 256, 0, s>>>(nbx, part, st, H, ldh, dots, pass);
     GOAL_CHECK_LAUNCH();
     if constexpr (vec) k_update_v<T, TV, R / 4><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
     else k_update<T, TV, R><<<nbx, 256, 0, s>>>(n, V, n, w, dots, st, npart, pass);
@@ -1125,14 +1139,14 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
         GOAL_CHECK_LAUNCH();
         if (sweep2) {
           k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
-                                                         K.t32.ptr);
+                                                                 K.t32.ptr);
           GOAL_CHECK_LAUNCH();
           k_second_sweep_col<float, __half><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V16.ptr, n, K.t32.ptr,
                                                                      K.r32.ptr, 0, sti);
           GOAL_CHECK_LAUNCH();
         }
         k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
-                                                       K.w32.ptr);
+                                                               K.w32.ptr);
         GOAL_CHECK_LAUNCH();
         arnoldi_orth<float, __half>(n, K.V16.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots32, red32, mi, 0.0,
                                     kInnerPasses, s);
