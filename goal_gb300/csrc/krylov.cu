@@ -272,6 +272,38 @@ __global__ void __launch_bounds__(256) k_spmv_col(int N, const int* __restrict__
     y[4ll * n + r] = block_row_dot<T, TA>(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r);
 }
 
+// First half of the learned preconditioner's step, fused: t = A z1 for the
+// node (z1 = x, the block-Jacobi sweep of v_j), then z = z1 + B (v_j - t).
+// The node's four rows are the four lanes of a quad, which exchange their t
+// by shuffles. z goes to out, not over x: other quads still read z1. Same
+// arithmetic as k_spmv_col followed by k_second_sweep_col.
+template <typename T, typename TA, typename TV>
+__global__ void __launch_bounds__(256, 8) k_spmv_sweep(int N, const int* __restrict__ brow_ptr,
+                                                    const int* __restrict__ bcol, const TA* __restrict__ A,
+                                                    const T* __restrict__ x, const T* __restrict__ B, const TV* V,
+                                                    long long ldv, const GState* st, T* __restrict__ out) {
+  if (st->done) return;
+  const TV* v = V + (long long)st->j * ldv;
+  const int lane = threadIdx.x & 31, r = lane & 3, q0 = lane & ~3;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int nb = warp * 8; nb < N; nb += nwarps * 8) {
+    const int n = nb + (lane >> 2);
+    const bool live = n < N;
+    const T t = live ? block_row_dot<T, TA>(bcol, A, x, __ldg(brow_ptr + n), __ldg(brow_ptr + n + 1), r) : T(0);
+    const T w0 = __shfl_sync(0xffffffffu, t, q0), w1 = __shfl_sync(0xffffffffu, t, q0 + 1);
+    const T w2 = __shfl_sync(0xffffffffu, t, q0 + 2), w3 = __shfl_sync(0xffffffffu, t, q0 + 3);
+    if (live) {
+      T b0, b1, b2, b3, v0, v1, v2, v3;
+      Vec4<T>::load(B + 16ll * n + 4 * r, b0, b1, b2, b3);
+      load_row<T, TV>(v + 4ll * n, v0, v1, v2, v3);
+      T z = x[4ll * n + r];
+      z += b0 * (v0 - w0) + b1 * (v1 - w1) + b2 * (v2 - w2) + b3 * (v3 - w3);
+      out[4ll * n + r] = z;
+    }
+  }
+}
+
 // Orthogonalization kernels work on row slabs of 256 x R rows per block:
 // every thread keeps its R entries of w in registers, and the
 // columns of V are streamed slab by slab (long contiguous reads, w read once).
@@ -653,6 +685,32 @@ __global__ void k_norm_givens(int nbx, const C* part, GState* st, C* H, int ldh,
   for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) h[i] = sh[i];
 }
 
+// V_j = w / hnext after k_norm_givens advanced j, and out = Dinv V_j (the
+// block-Jacobi sweep of the next Arnoldi step, from the stored entries): one
+// node (four rows) per thread
+template <typename T, typename TV>
+__global__ void k_normalize_next_bj(long long n, TV* V, long long ld, const T* w, const GState* st,
+                                    const T* __restrict__ Dinv, T* __restrict__ out) {
+  if (st->done) return;
+  const T inv = state_inv<T>(st);
+  TV* v = V + (long long)st->j * ld;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; 4 * q < n; q += (long long)gridDim.x * blockDim.x) {
+    T a, b, c, d;
+    Vec4<T>::load(w + 4 * q, a, b, c, d);
+    Vec4Store<TV>::store(v + 4 * q, a * inv, b * inv, c * inv, d * inv);
+    T x0, x1, x2, x3;
+    load_row<T, TV>(v + 4 * q, x0, x1, x2, x3);
+    T r[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      T d0, d1, d2, d3;
+      Vec4<T>::load(Dinv + 16 * q + 4 * e, d0, d1, d2, d3);
+      r[e] = d0 * x0 + d1 * x1 + d2 * x2 + d3 * x3;
+    }
+    Vec4Store<T>::store(out + 4 * q, r[0], r[1], r[2], r[3]);
+  }
+}
+
 // V_j = w / hnext after k_norm_givens advanced j
 template <typename T, typename TV>
 __global__ void k_normalize_next(long long n, TV* V, long long ld, const T* w, const GState* st) {
@@ -988,9 +1046,11 @@ void orth_passes(long long n, TV* V, T* w, GState* st, T* H, int ldh, T* dots, T
 
 // One Arnoldi step's orthogonalization (CGS with a conditional second pass),
 // normalization and Givens update, on state st.
+// bj_D / bj_out (single pass only): also out = Dinv V_{j+1}, the first sweep
+// of the next step's preconditioner.
 template <typename T, typename TV>
 void arnoldi_orth(long long n, TV* V, T* w, GState* st, T* H, int ldh, T* cs, T* sn, T* g, T* dots, T* red, int jmax,
-                  double tol_abs, int passes, cudaStream_t s) {
+                  double tol_abs, int passes, cudaStream_t s, const T* bj_D = nullptr, T* bj_out = nullptr) {
   switch (orth_rows<T, TV>(n)) {
     case 1: orth_passes<T, TV, 1>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
     case 2: orth_passes<T, TV, 2>(n, V, w, st, H, ldh, dots, red, jmax, passes, s); break;
@@ -1007,7 +1067,8 @@ void arnoldi_orth(long long n, TV* V, T* w, GState* st, T* H, int ldh, T* cs, T*
     const int nbx = slab_grid(n, orth_rows<T, TV>(n));
     k_norm_givens<T><<<1, 256, 0, s>>>(nbx, red + (size_t)(kMaxM + 2) * nbx, st, H, ldh, cs, sn, g, jmax, tol_abs);
     GOAL_CHECK_LAUNCH();
-    k_normalize_next<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st);
+    if (bj_D) k_normalize_next_bj<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st, bj_D, bj_out);
+    else k_normalize_next<T, TV><<<vec_grid(n / 4), 256, 0, s>>>(n, V, n, w, st);
     GOAL_CHECK_LAUNCH();
   }
 }
@@ -1133,23 +1194,23 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
       GOAL_CHECK_LAUNCH();
       k_scale_into<__half, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V16.ptr);
       GOAL_CHECK_LAUNCH();
+      // r32 = D^-1 v_0; later steps get D^-1 v_it from the normalization
+      k_bj_colin<float, __half><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V16.ptr, n, sti, K.r32.ptr);
+      GOAL_CHECK_LAUNCH();
       for (int it = 0; it < mi; ++it) {
-        // r32 = M^-1 v_it ; w32 = A^ r32 (ld 0 keeps the input at r32)
-        k_bj_colin<float, __half><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V16.ptr, n, sti, K.r32.ptr);
-        GOAL_CHECK_LAUNCH();
+        // z = M^-1 v_it (in t32 with the second sweep, else r32); w32 = A^ z
+        float* z = K.r32.ptr;
         if (sweep2) {
-          k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
-                                                                 K.t32.ptr);
+          k_spmv_sweep<float, __half, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr,
+                                                                           K.Bc32.ptr, K.V16.ptr, n, sti, K.t32.ptr);
           GOAL_CHECK_LAUNCH();
-          k_second_sweep_col<float, __half><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.V16.ptr, n, K.t32.ptr,
-                                                                     K.r32.ptr, 0, sti);
-          GOAL_CHECK_LAUNCH();
+          z = K.t32.ptr;
         }
-        k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, 0, sti,
-                                                               K.w32.ptr);
+        k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, z, 0, sti, K.w32.ptr);
         GOAL_CHECK_LAUNCH();
+        // orthogonalize, normalize into v_{it+1}, and r32 = D^-1 v_{it+1}
         arnoldi_orth<float, __half>(n, K.V16.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots32, red32, mi, 0.0,
-                                    kInnerPasses, s);
+                                    kInnerPasses, s, K.Dinv32.ptr, K.r32.ptr);
       }
       k_backsolve<float><<<1, 32, 0, s>>>(sti, Hin, mi + 1, gin, yin);
       GOAL_CHECK_LAUNCH();
