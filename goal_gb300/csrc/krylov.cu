@@ -940,11 +940,12 @@ int slab_rows(long long n) {
   return r;
 }
 int slab_grid(long long n, int rows) { return (int)std::max(1ll, (n + 256ll * rows - 1) / (256ll * rows)); }
-// a binary16 basis is read in groups of four rows: at least 4 rows per thread
+// a binary16 basis is read in groups of four rows: 4 rows per thread, or 8
+// once 4 would need more than one wave of eight 256-thread blocks per SM
 template <typename T, typename TV>
 int orth_rows(long long n) {
-  const int r = slab_rows<T>(n);
-  return std::is_same<TV, __half>::value ? std::max(r, 4) : r;
+  if (!std::is_same<TV, __half>::value) return slab_rows<T>(n);
+  return n > 1024ll * 8 * kSMs ? 8 : 4;
 }
 
 }  // namespace
