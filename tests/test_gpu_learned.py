@@ -95,6 +95,15 @@ def test_training_and_gain_over_block_jacobi():
     assert plain["converged"] and learned["converged"]
     assert learned["iters"] < 0.8 * plain["iters"]
     assert np.linalg.norm(x1 - x0) <= 1e-7 * np.linalg.norm(x0)
+    # the learned two-sweep inside the FP32-inner / FP64-outer solve: the same
+    # solution, fewer outer iterations than plain block-Jacobi in that solver,
+    # and bitwise repeatable (fixed reduction orders, no atomics)
+    pm = dict(prm, krylov_size=30, precision=api.MIXED, inner_iters=30)
+    x3, lm = api.solve(s, b, params=api.solve_params(precond=api.PRECOND_LEARNED, **pm))
+    x4, lm2 = api.solve(s, b, params=api.solve_params(precond=api.PRECOND_LEARNED, **pm))
+    assert lm["converged"] and not lm["fell_back"]
+    assert np.array_equal(x3, x4) and lm["iters"] == lm2["iters"]
+    assert np.linalg.norm(x3 - x0) <= 1e-7 * np.linalg.norm(x0)
     # cap: stop the learned run early and finish with plain block-Jacobi
     x2, capped = api.solve(s, b, params=api.solve_params(precond=api.PRECOND_LEARNED, learned_cap=5, **prm))
     assert capped["fell_back"] and capped["converged"]

@@ -68,6 +68,12 @@ def test_mixed_needs_fewer_outer_iterations():
                                                      inner_iters=30))
     assert s64["converged"] and smx["converged"]
     assert smx["iters"] < s64["iters"]
+    # the mixed solve is bitwise repeatable
+    x1, s1 = api.solve(s, b, params=api.solve_params(tolerance=1e-10, max_iters=5000, precision=api.MIXED,
+                                                     inner_iters=30))
+    x2, s2 = api.solve(s, b, params=api.solve_params(tolerance=1e-10, max_iters=5000, precision=api.MIXED,
+                                                     inner_iters=30))
+    assert np.array_equal(x1, x2) and s1["iters"] == s2["iters"]
 
 
 @pytest.mark.parametrize("case", ["neohookean_uniaxial_3D", "J2_uniaxial_3D", "J2_traction_3D"])
