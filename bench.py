@@ -465,8 +465,8 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7):
     (rho = 20): per cycle the Newton solve, five timed R+J assemblies, the
     nested adjoint solved to 1e-10 with FP32-inner / FP64-outer FGMRES (plain
     block-Jacobi, then the network trained on this cycle's Newton Jacobian),
-    the DWR estimate, the size field for growth x elements, and the refinement
-    with the fields carried over."""
+    the DWR estimate, the size field for growth x elements, and the adaptation
+    (coarsening, then refinement) with the fields carried over."""
     import torch
     from goal_gb300 import adapt
     from goal_gb300.mesh import graded_block
@@ -526,11 +526,12 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7):
             states = {"sigma": m.get_state(api.SIGMA), "Fp": m.get_state(api.FP), "Fp_old": m.get_state(api.FP_OLD),
                       "eqps": m.get_state(api.EQPS), "eqps_old": m.get_state(api.EQPS_OLD)}
             t1 = time.perf_counter()
-            mesh, parents, origin = adapt.refine_to_size(mesh, size)
-            rec["refine_seconds"] = time.perf_counter() - t1
+            mesh, tr = adapt.adapt_to_size(mesh, size)
+            rec["adapt_seconds"] = time.perf_counter() - t1
+            rec["coarsened_elements"] = int(len(tr.elem_origin_c))
             rec["target"] = target
-            U = adapt.transfer_nodal(U, parents)
-            states = adapt.transfer_states(states, origin)
+            U = tr.nodal(U)
+            states = tr.states(states)
         out.append(rec)
     return out
 

@@ -1,15 +1,18 @@
-"""Mesh refinement to a target size field and the transfer of the solution
-and states onto the refined mesh: the adaptation step of goal's nested loop
+"""Mesh adaptation to a target size field and the transfer of the solution
+and states onto the adapted mesh: the adaptation step of goal's nested loop
 (src/main_nested.cpp:106-126). goal remeshes with SCOREC ma::adapt (not part
-of the reference); here the mesh is refined by conforming longest-edge
-bisection (``goal_refiner_*`` in the C ABI), driven by the isotropic target
-size field of the DWR indicators (``api.size_field``, src/goal_size_field.cpp).
+of the reference); here the mesh is coarsened by edge collapse
+(``goal_coarsener_*`` in the C ABI) and refined by conforming longest-edge
+bisection (``goal_refiner_*``), driven by the isotropic target size field of
+the DWR indicators (``api.size_field``, src/goal_size_field.cpp).
 
 Transfer rules (the same as goal's nested-mesh rules, src/goal_nested.cpp:347-393):
 a new node, at the midpoint of an edge, takes the mean of the edge's end
 point values (exact for the linear fields); a child element takes its parent
 element's integration-point states. A new node belongs to a node set when
 both end points of its edge do; side triangles are split with their edges.
+Coarsening keeps a subset of the nodes, which keep their values, and a subset
+of the elements (with one node moved), which keep their states.
 """
 from __future__ import annotations
 
@@ -66,6 +69,106 @@ def refine_to_size(mesh: Mesh, vtx_size: np.ndarray, ratio: float = 1.5, max_ele
     out = Mesh(coords=X, tets=T, elem_set=np.asarray(mesh.elem_set)[org].astype(np.int32),
                elem_set_names=list(mesh.elem_set_names), node_sets=node_sets, side_sets=side_sets)
     return out, new_parents, org
+
+
+def _node_class(mesh: Mesh) -> np.ndarray:
+    """Per-node bit mask of node-set (bit k, k < 30) and side-set (bit 30 + k)
+    memberships, for the coarsening rule that a collapsed node's sets are a
+    subset of its target's."""
+    cls = np.zeros(mesh.num_nodes, np.int64)
+    for k, name in enumerate(sorted(mesh.node_sets)[:30]):
+        cls[np.asarray(mesh.node_sets[name], np.int64)] |= np.int64(1) << k
+    for k, name in enumerate(sorted(mesh.side_sets)[:30]):
+        tri = np.asarray(mesh.side_sets[name], np.int64).reshape(-1)
+        cls[np.unique(tri)] |= np.int64(1) << (30 + k)
+    return cls
+
+
+def coarsen_to_size(mesh: Mesh, vtx_size: np.ndarray, ratio: float = 0.5, refine_ratio: float = 1.5,
+                    min_quality: float = 0.2, max_passes: int = 8) -> Tuple[Mesh, np.ndarray, np.ndarray]:
+    """Collapses edges shorter than ``ratio`` times the mean target size of
+    their end points (``goal_coarsener_*``: model and validity checks there).
+    Returns the coarsened mesh, the original node of each kept node and the
+    original element of each kept element."""
+    L = lib()
+    N, E = mesh.num_nodes, mesh.num_elems
+    size = _f64(vtx_size)
+    if size.shape != (N,):
+        raise ValueError("one target size per node")
+    names = sorted(mesh.side_sets)
+    tris = [np.asarray(mesh.side_sets[k], np.int32).reshape(-1, 3) for k in names]
+    tri = np.ascontiguousarray(np.concatenate(tris) if tris else np.zeros((0, 3), np.int32), dtype=np.int32)
+    tri_set = np.ascontiguousarray(np.concatenate([np.full(len(t), i, np.int32) for i, t in enumerate(tris)])
+                                   if tris else np.zeros(0, np.int32))
+    coords = _f64(mesh.coords)
+    tets = _i32(mesh.tets)
+    eset = _i32(mesh.elem_set)
+    cls = np.ascontiguousarray(_node_class(mesh))
+    h = ctypes.c_void_p()
+    check(L.goal_coarsener_create(N, _ptr(coords), E, _ptr(tets), _ptr(eset), _ptr(cls), len(tri), _ptr(tri),
+                                  _ptr(tri_set), ctypes.byref(h)))
+    try:
+        sizes = (ctypes.c_longlong * 3)()
+        check(L.goal_coarsener_coarsen(h, _ptr(size), float(ratio), float(refine_ratio), float(min_quality),
+                                       int(max_passes), sizes))
+        n2, e2, s2 = int(sizes[0]), int(sizes[1]), int(sizes[2])
+        X = np.zeros((n2, 3))
+        org_n = np.zeros(n2, np.int32)
+        T = np.zeros((e2, 4), np.int32)
+        org_e = np.zeros(e2, np.int32)
+        tri2 = np.zeros((s2, 3), np.int32)
+        tset2 = np.zeros(s2, np.int32)
+        check(L.goal_coarsener_get(h, _ptr(X), _ptr(org_n), _ptr(T), _ptr(org_e), _ptr(tri2), _ptr(tset2)))
+    finally:
+        L.goal_coarsener_destroy(h)
+    renum = np.full(N, -1, np.int64)
+    renum[org_n] = np.arange(n2)
+    node_sets = {}
+    for name, nodes in mesh.node_sets.items():
+        kept = renum[np.asarray(nodes, np.int64)]
+        node_sets[name] = np.sort(kept[kept >= 0]).astype(np.int32)
+    side_sets = {name: tri2[tset2 == i] for i, name in enumerate(names)}
+    out = Mesh(coords=X, tets=T, elem_set=np.asarray(mesh.elem_set)[org_e].astype(np.int32),
+               elem_set_names=list(mesh.elem_set_names), node_sets=node_sets, side_sets=side_sets)
+    return out, org_n, org_e
+
+
+class Transfer:
+    """Moves nodal fields and element states from the mesh before an
+    adaptation to the mesh after it: through the coarsening (kept nodes keep
+    their values, kept elements their states), then the refinement (midpoint
+    means, children inherit)."""
+
+    def __init__(self, node_origin: np.ndarray, elem_origin_c: np.ndarray, new_parents: np.ndarray,
+                 elem_origin_r: np.ndarray):
+        self.node_origin = node_origin
+        self.elem_origin_c = elem_origin_c
+        self.new_parents = new_parents
+        self.elem_origin_r = elem_origin_r
+
+    def nodal(self, values: np.ndarray) -> np.ndarray:
+        v = np.asarray(values, np.float64)
+        return transfer_nodal(v.reshape(len(v), -1)[self.node_origin], self.new_parents)
+
+    def states(self, states: Dict[str, np.ndarray]) -> Dict[str, np.ndarray]:
+        return transfer_states(transfer_states(states, self.elem_origin_c), self.elem_origin_r)
+
+    @property
+    def elem_origin(self) -> np.ndarray:
+        """The original element of every element of the adapted mesh."""
+        return np.asarray(self.elem_origin_c)[self.elem_origin_r]
+
+
+def adapt_to_size(mesh: Mesh, vtx_size: np.ndarray, coarsen_ratio: float = 0.5, refine_ratio: float = 1.5,
+                  min_quality: float = 0.2, max_elems: int = 50_000_000) -> Tuple[Mesh, Transfer]:
+    """One adaptation to a size field: coarsen (edges shorter than
+    coarsen_ratio x size), then refine (edges longer than refine_ratio x
+    size). Returns the adapted mesh and the transfer of fields onto it."""
+    size = _f64(vtx_size)
+    mc, org_n, org_ec = coarsen_to_size(mesh, size, ratio=coarsen_ratio, refine_ratio=refine_ratio,
+                                        min_quality=min_quality)
+    mr, parents, org_er = refine_to_size(mc, size[org_n], ratio=refine_ratio, max_elems=max_elems)
+    return mr, Transfer(org_n, org_ec, parents, org_er)
 
 
 def _propagate(arr, base, new_parents, combine):

@@ -13,9 +13,9 @@ and the regression check (src/goal_regression.cpp:14-23), with goal's log lines
 functional and the output; before every cycle but the last, NestedAdjoint::run
 on the uniformly refined mesh (`z.R = %.15e`, `|J(u)-J(uh)| < %.15e`), the
 isotropic target size field (src/goal_size_field.cpp) for "target elems" x
-"target growth"^(cycle-1), and the refinement of the mesh to that size with
-the solution and states carried over (goal_gb300.adapt; goal remeshes with
-SCOREC ma::adapt, which also coarsens -- this refines only).
+"target growth"^(cycle-1), and the adaptation of the mesh to that size
+(edge-collapse coarsening, then longest-edge bisection) with the solution and
+states carried over (goal_gb300.adapt; goal remeshes with SCOREC ma::adapt).
 
 3D meshes in SCOREC SMB v5 with their .dmg model and association file, the
 package's .npz mesh file, or a restart directory written with "write native";
@@ -106,16 +106,17 @@ class _Setup:
             self.output.mesh, self.output.mech = mesh, self.mech
 
     def adapt_to(self, size, ratio=1.5):
-        """Refines to the target size field and moves the solution and the
-        states onto the refined mesh (the remeshing of Solver::adapt,
-        src/main_nested.cpp:106-126, with goal's field transfer)."""
+        """Adapts the mesh to the target size field (coarsening, then
+        refinement) and moves the solution and the states onto it (the
+        remeshing of Solver::adapt, src/main_nested.cpp:106-126, with goal's
+        field transfer)."""
         from . import adapt
         U = self.mech.get_solution().reshape(-1, 4)
         states = {n: self.mech.get_state(w) for n, w, _ in output.STATE_FIELDS
                   if self.model == api.J2 or w == api.SIGMA}
-        mesh, parents, origin = adapt.refine_to_size(self.mesh, size, ratio=ratio)
-        U2 = adapt.transfer_nodal(U, parents)
-        st2 = adapt.transfer_states(states, origin)
+        mesh, tr = adapt.adapt_to_size(self.mesh, size, refine_ratio=ratio)
+        U2 = tr.nodal(U)
+        st2 = tr.states(states)
         self.build(mesh)
         self.mech.set_solution(U2.ravel())
         ids = {n: w for n, w, _ in output.STATE_FIELDS}

@@ -1,0 +1,487 @@
+// Coarsening of a tetrahedral mesh to a target size field by edge collapse,
+// the coarsening half of goal's adaptation loop (src/main_nested.cpp:106-126,
+// which calls SCOREC ma::adapt -- not part of the reference tree). An edge
+// (a, b) shorter than ratio x (mean target size of its end points) is
+// collapsed by moving b onto a. A collapse is taken only if it keeps the
+// model: the node / side sets b belongs to (node_class bits) are a subset of
+// a's, b is not on an element-set interface, a boundary b is on a flat part of
+// the boundary and (a, b) is a boundary edge; and only if it keeps the mesh
+// valid: the link condition (no fold-over of the topology), every remaining
+// tet around b positively oriented with mean-ratio quality at least
+// min(min_quality, the worst quality around b before), and no new edge longer
+// than refine_ratio x its mean target size (the refinement would split it
+// again). Candidates go shortest (relative to size) first, one independent set
+// of collapses per pass; ties break on the end-point pair, so the result is
+// deterministic.
+//
+// Host code: a sequence of local topological updates; the discretization built
+// from its output goes back to the GPU.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <memory>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/goal_gb300.h"
+#include "common.cuh"
+
+namespace goal {
+namespace {
+
+constexpr long long kBoundaryBit = 1ll << 62;
+
+inline uint64_t ekey(int a, int b) {
+  const uint64_t lo = (uint64_t)(unsigned)std::min(a, b), hi = (uint64_t)(unsigned)std::max(a, b);
+  return (hi << 32) | lo;
+}
+
+struct Coarsener {
+  int N = 0;
+  std::vector<double> X;
+  std::vector<long long> cls;
+  std::vector<double> size;
+  std::vector<char> valive;
+  std::vector<std::array<int, 4>> T;
+  std::vector<int> eset;
+  std::vector<char> talive;
+  std::vector<std::vector<int>> vt;  // vertex -> tets (live ones; dead entries are filtered on use)
+  // boundary faces (faces of exactly one tet) and side triangles
+  std::vector<std::array<int, 3>> F;
+  std::vector<char> falive;
+  std::vector<std::vector<int>> vf;
+  std::vector<std::array<int, 3>> S;
+  std::vector<int> S_set;
+  std::vector<char> salive;
+  std::vector<std::vector<int>> vs;
+
+  double len2(int a, int b) const {
+    const double dx = X[3 * a] - X[3 * b], dy = X[3 * a + 1] - X[3 * b + 1], dz = X[3 * a + 2] - X[3 * b + 2];
+    return dx * dx + dy * dy + dz * dz;
+  }
+  // signed volume x 6 and mean-ratio quality 12 (3|V|)^(2/3) / sum l^2
+  double vol6(const std::array<int, 4>& v) const {
+    const double* p0 = &X[3 * v[0]];
+    double e[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) e[k][c] = X[3 * v[k + 1] + c] - p0[c];
+    return e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) - e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+           e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+  }
+  double quality(const std::array<int, 4>& v) const {
+    const double V = vol6(v) / 6.0;
+    double l2 = 0.0;
+    for (int i = 0; i < 4; ++i)
+      for (int j = i + 1; j < 4; ++j) l2 += len2(v[i], v[j]);
+    if (!(V > 0.0) || !(l2 > 0.0)) return 0.0;
+    return 12.0 * std::cbrt(9.0 * V * V) / l2;
+  }
+  static void compact(std::vector<int>& list, const std::vector<char>& alive) {
+    list.erase(std::remove_if(list.begin(), list.end(), [&](int t) { return !alive[t]; }), list.end());
+  }
+  bool has(const std::array<int, 4>& v, int x) const { return v[0] == x || v[1] == x || v[2] == x || v[3] == x; }
+  static bool has3(const std::array<int, 3>& v, int x) { return v[0] == x || v[1] == x || v[2] == x; }
+  bool boundary(int v) const { return (cls[v] & kBoundaryBit) != 0; }
+
+  void normal(const std::array<int, 3>& f, double n[3]) const {
+    double u[3], w[3];
+    for (int c = 0; c < 3; ++c) {
+      u[c] = X[3 * f[1] + c] - X[3 * f[0] + c];
+      w[c] = X[3 * f[2] + c] - X[3 * f[0] + c];
+    }
+    n[0] = u[1] * w[2] - u[2] * w[1];
+    n[1] = u[2] * w[0] - u[0] * w[2];
+    n[2] = u[0] * w[1] - u[1] * w[0];
+    const double m = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int c = 0; c < 3; ++c) n[c] = m > 0.0 ? n[c] / m : 0.0;
+  }
+
+  // vertices sharing a live tet with v
+  void adjacent(int v, std::vector<int>& out) const {
+    out.clear();
+    for (int t : vt[v])
+      if (talive[t])
+        for (int x : T[t])
+          if (x != v) out.push_back(x);
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+  }
+
+  // can b be moved onto a?
+  bool can_collapse(int b, int a, double refine_ratio, double min_quality) const {
+    if ((cls[b] & ~cls[a]) != 0) return false;
+    // element sets: b inside one set
+    int es = -1;
+    for (int t : vt[b]) {
+      if (!talive[t]) continue;
+      if (es < 0) es = eset[t];
+      else if (eset[t] != es) return false;
+    }
+    // boundary b: flat, and (a, b) a boundary edge
+    if (boundary(b)) {
+      bool edge_on_boundary = false;
+      double n0[3] = {0, 0, 0};
+      bool first = true;
+      for (int f : vf[b]) {
+        if (!falive[f]) continue;
+        if (has3(F[f], a)) edge_on_boundary = true;
+        double n[3];
+        normal(F[f], n);
+        if (first) {
+          for (int c = 0; c < 3; ++c) n0[c] = n[c];
+          first = false;
+        } else if (std::fabs(n[0] * n0[0] + n[1] * n0[1] + n[2] * n0[2]) < 1.0 - 1e-10) {
+          return false;
+        }
+      }
+      if (!edge_on_boundary) return false;
+    }
+    // link condition: the vertices adjacent to both a and b are exactly the
+    // vertices of the tets around edge ab; edges (c, d) seen from both a and b
+    // must belong to a tet around ab
+    std::vector<int> adj_a, adj_b;
+    adjacent(a, adj_a);
+    adjacent(b, adj_b);
+    if (!std::binary_search(adj_b.begin(), adj_b.end(), a)) return false;
+    std::vector<int> common;
+    std::set_intersection(adj_a.begin(), adj_a.end(), adj_b.begin(), adj_b.end(), std::back_inserter(common));
+    std::vector<int> lab;
+    std::unordered_set<uint64_t> elab;
+    for (int t : vt[b]) {
+      if (!talive[t] || !has(T[t], a)) continue;
+      int cd[2], k = 0;
+      for (int x : T[t])
+        if (x != a && x != b) cd[k++] = x;
+      lab.push_back(cd[0]);
+      lab.push_back(cd[1]);
+      elab.insert(ekey(cd[0], cd[1]));
+    }
+    std::sort(lab.begin(), lab.end());
+    lab.erase(std::unique(lab.begin(), lab.end()), lab.end());
+    if (common != lab) return false;
+    {
+      std::unordered_set<uint64_t> ea;
+      for (int t : vt[a]) {
+        if (!talive[t] || has(T[t], b)) continue;
+        int cd[3], k = 0;
+        for (int x : T[t])
+          if (x != a) cd[k++] = x;
+        ea.insert(ekey(cd[0], cd[1]));
+        ea.insert(ekey(cd[0], cd[2]));
+        ea.insert(ekey(cd[1], cd[2]));
+      }
+      for (int t : vt[b]) {
+        if (!talive[t] || has(T[t], a)) continue;
+        int cd[3], k = 0;
+        for (int x : T[t])
+          if (x != b) cd[k++] = x;
+        const uint64_t e3[3] = {ekey(cd[0], cd[1]), ekey(cd[0], cd[2]), ekey(cd[1], cd[2])};
+        for (uint64_t e : e3)
+          if (ea.count(e) && !elab.count(e)) return false;
+      }
+    }
+    // the same on the boundary surface: a boundary vertex c joined to both a
+    // and b by boundary edges must make a boundary face with them
+    if (boundary(a) && boundary(b)) {
+      std::vector<int> ca, cb, fab;
+      for (int f : vf[a])
+        if (falive[f] && !has3(F[f], b))
+          for (int x : F[f])
+            if (x != a) ca.push_back(x);
+      for (int f : vf[b])
+        if (falive[f]) {
+          if (has3(F[f], a)) {
+            for (int x : F[f])
+              if (x != a && x != b) fab.push_back(x);
+          } else {
+            for (int x : F[f])
+              if (x != b) cb.push_back(x);
+          }
+        }
+      std::sort(ca.begin(), ca.end());
+      std::sort(cb.begin(), cb.end());
+      std::vector<int> both;
+      std::set_intersection(ca.begin(), ca.end(), cb.begin(), cb.end(), std::back_inserter(both));
+      for (int c : both)
+        if (std::find(fab.begin(), fab.end(), c) == fab.end()) return false;
+    }
+    // geometry: the tets that keep b (as a) stay valid and good enough; no
+    // new edge too long
+    double worst = 1.0;
+    for (int t : vt[b])
+      if (talive[t]) worst = std::min(worst, quality(T[t]));
+    const double qmin = std::min(min_quality, worst);
+    for (int t : vt[b]) {
+      if (!talive[t] || has(T[t], a)) continue;
+      std::array<int, 4> v = T[t];
+      for (int& x : v)
+        if (x == b) x = a;
+      if (!(vol6(v) > 0.0) || quality(v) < qmin) return false;
+    }
+    for (int c : adj_b) {
+      if (c == a) continue;
+      const double s = refine_ratio * 0.5 * (size[a] + size[c]);
+      if (len2(a, c) > s * s) return false;
+    }
+    return true;
+  }
+
+  void collapse(int b, int a) {
+    for (int t : vt[b]) {
+      if (!talive[t]) continue;
+      if (has(T[t], a)) {
+        talive[t] = 0;
+        continue;
+      }
+      for (int& x : T[t])
+        if (x == b) x = a;
+      vt[a].push_back(t);
+    }
+    vt[b].clear();
+    for (int f : vf[b]) {
+      if (!falive[f]) continue;
+      if (has3(F[f], a)) {
+        falive[f] = 0;
+        continue;
+      }
+      for (int& x : F[f])
+        if (x == b) x = a;
+      vf[a].push_back(f);
+    }
+    vf[b].clear();
+    for (int f : vs[b]) {
+      if (!salive[f]) continue;
+      if (has3(S[f], a)) {
+        salive[f] = 0;
+        continue;
+      }
+      for (int& x : S[f])
+        if (x == b) x = a;
+      vs[a].push_back(f);
+    }
+    vs[b].clear();
+    valive[b] = 0;
+    compact(vt[a], talive);
+    compact(vf[a], falive);
+    compact(vs[a], salive);
+  }
+
+  int pass(double ratio, double refine_ratio, double min_quality) {
+    struct Cand {
+      double r;
+      uint64_t key;
+    };
+    std::vector<Cand> cand;
+    std::unordered_set<uint64_t> seen;
+    for (size_t t = 0; t < T.size(); ++t) {
+      if (!talive[t]) continue;
+      const auto& v = T[t];
+      for (int i = 0; i < 4; ++i)
+        for (int j = i + 1; j < 4; ++j) {
+          const uint64_t k = ekey(v[i], v[j]);
+          if (!seen.insert(k).second) continue;
+          const double s = 0.5 * (size[v[i]] + size[v[j]]);
+          const double r = std::sqrt(len2(v[i], v[j])) / s;
+          if (r < ratio) cand.push_back({r, k});
+        }
+    }
+    std::sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) {
+      return x.r != y.r ? x.r < y.r : x.key < y.key;
+    });
+    std::vector<char> touched(N, 0);
+    std::vector<int> adj;
+    int done = 0;
+    for (const Cand& c : cand) {
+      const int lo = (int)(c.key & 0xffffffffu), hi = (int)(c.key >> 32);
+      if (!valive[lo] || !valive[hi] || touched[lo] || touched[hi]) continue;
+      int b = -1, a = -1;
+      if (can_collapse(hi, lo, refine_ratio, min_quality)) { b = hi; a = lo; }
+      else if (can_collapse(lo, hi, refine_ratio, min_quality)) { b = lo; a = hi; }
+      if (b < 0) continue;
+      adjacent(b, adj);
+      touched[a] = touched[b] = 1;
+      for (int x : adj) touched[x] = 1;
+      collapse(b, a);
+      ++done;
+    }
+    return done;
+  }
+};
+
+}  // namespace
+}  // namespace goal
+
+struct goal_coarsener_s {
+  goal::Coarsener c;
+};
+
+extern "C" {
+
+int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, const int* tets, const int* elem_set,
+                          const long long* node_class, int num_sides, const int* tris, const int* tri_set,
+                          goal_coarsener* out) {
+  try {
+    if (!out || !coords || !tets || !node_class || num_nodes <= 0 || num_elems <= 0 ||
+        (num_sides > 0 && (!tris || !tri_set)))
+      throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_create: bad arguments");
+    auto h = std::make_unique<goal_coarsener_s>();
+    goal::Coarsener& c = h->c;
+    c.N = num_nodes;
+    c.X.assign(coords, coords + 3ll * num_nodes);
+    c.cls.assign(node_class, node_class + num_nodes);
+    for (long long& x : c.cls) x &= ~goal::kBoundaryBit;
+    c.size.assign(num_nodes, 0.0);
+    c.valive.assign(num_nodes, 1);
+    c.T.resize(num_elems);
+    c.eset.assign(num_elems, 0);
+    c.talive.assign(num_elems, 1);
+    c.vt.assign(num_nodes, {});
+    c.vf.assign(num_nodes, {});
+    c.vs.assign(num_nodes, {});
+    // boundary faces: the faces of exactly one tet
+    struct FaceRec {
+      std::array<int, 3> v;
+      int count;
+    };
+    std::unordered_map<uint64_t, std::vector<FaceRec>> faces;
+    auto fkey = [](std::array<int, 3> s) {
+      std::sort(s.begin(), s.end());
+      return ((uint64_t)(unsigned)s[0] * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)(unsigned)s[1] << 21) ^
+             ((uint64_t)(unsigned)s[2] << 42) ^ (uint64_t)(unsigned)s[2];
+    };
+    static const int kFaces[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
+    for (int e = 0; e < num_elems; ++e) {
+      for (int q = 0; q < 4; ++q) {
+        const int v = tets[4ll * e + q];
+        if (v < 0 || v >= num_nodes) throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_create: node id out of range");
+        c.T[e][q] = v;
+        c.vt[v].push_back(e);
+      }
+      c.eset[e] = elem_set ? elem_set[e] : 0;
+      for (auto& fq : kFaces) {
+        std::array<int, 3> f = {c.T[e][fq[0]], c.T[e][fq[1]], c.T[e][fq[2]]};
+        std::array<int, 3> sf = f;
+        std::sort(sf.begin(), sf.end());
+        auto& bucket = faces[fkey(f)];
+        bool found = false;
+        for (auto& r : bucket) {
+          std::array<int, 3> sr = r.v;
+          std::sort(sr.begin(), sr.end());
+          if (sr == sf) {
+            ++r.count;
+            found = true;
+            break;
+          }
+        }
+        if (!found) bucket.push_back({f, 1});
+      }
+    }
+    std::vector<std::array<int, 3>> bfaces;
+    for (auto& kv : faces)
+      for (auto& r : kv.second)
+        if (r.count == 1) bfaces.push_back(r.v);
+    std::sort(bfaces.begin(), bfaces.end());  // deterministic order
+    for (const auto& f : bfaces) {
+      const int id = (int)c.F.size();
+      c.F.push_back(f);
+      c.falive.push_back(1);
+      for (int v : f) {
+        c.vf[v].push_back(id);
+        c.cls[v] |= goal::kBoundaryBit;
+      }
+    }
+    for (int f = 0; f < num_sides; ++f) {
+      std::array<int, 3> s = {tris[3ll * f], tris[3ll * f + 1], tris[3ll * f + 2]};
+      for (int v : s)
+        if (v < 0 || v >= num_nodes) throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_create: side node out of range");
+      c.S.push_back(s);
+      c.S_set.push_back(tri_set[f]);
+      c.salive.push_back(1);
+      for (int v : s) c.vs[v].push_back(f);
+    }
+    *out = h.release();
+  } catch (const goal::Error& e) {
+    goal::set_last_error(e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    goal::set_last_error(e.what());
+    return GOAL_ERR_STATE;
+  }
+  return GOAL_OK;
+}
+
+int goal_coarsener_coarsen(goal_coarsener h, const double* vtx_size, double ratio, double refine_ratio,
+                           double min_quality, int max_passes, long long* sizes) {
+  try {
+    if (!h || !vtx_size || !sizes || !(ratio > 0.0) || !(refine_ratio > ratio) || !(min_quality >= 0.0))
+      throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_coarsen: bad arguments");
+    goal::Coarsener& c = h->c;
+    for (int n = 0; n < c.N; ++n) {
+      if (!(vtx_size[n] > 0.0)) throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_coarsen: sizes must be positive");
+      c.size[n] = vtx_size[n];
+    }
+    for (int p = 0; p < max_passes; ++p)
+      if (c.pass(ratio, refine_ratio, min_quality) == 0) break;
+    long long nn = 0, ne = 0, ns = 0;
+    for (char a : c.valive) nn += a ? 1 : 0;
+    for (char a : c.talive) ne += a ? 1 : 0;
+    for (char a : c.salive) ns += a ? 1 : 0;
+    sizes[0] = nn;
+    sizes[1] = ne;
+    sizes[2] = ns;
+  } catch (const goal::Error& e) {
+    goal::set_last_error(e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    goal::set_last_error(e.what());
+    return GOAL_ERR_STATE;
+  }
+  return GOAL_OK;
+}
+
+int goal_coarsener_get(goal_coarsener h, double* coords, int* node_origin, int* tets, int* elem_origin, int* tris,
+                       int* tri_set) {
+  try {
+    if (!h || !coords || !node_origin || !tets || !elem_origin)
+      throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_get: bad arguments");
+    const goal::Coarsener& c = h->c;
+    std::vector<int> renum(c.N, -1);
+    int k = 0;
+    for (int n = 0; n < c.N; ++n)
+      if (c.valive[n]) {
+        renum[n] = k;
+        node_origin[k] = n;
+        for (int q = 0; q < 3; ++q) coords[3ll * k + q] = c.X[3ll * n + q];
+        ++k;
+      }
+    long long e = 0;
+    for (size_t t = 0; t < c.T.size(); ++t)
+      if (c.talive[t]) {
+        for (int q = 0; q < 4; ++q) tets[4 * e + q] = renum[c.T[t][q]];
+        elem_origin[e] = (int)t;
+        ++e;
+      }
+    if (tris && tri_set) {
+      long long f = 0;
+      for (size_t s = 0; s < c.S.size(); ++s)
+        if (c.salive[s]) {
+          for (int q = 0; q < 3; ++q) tris[3 * f + q] = renum[c.S[s][q]];
+          tri_set[f] = c.S_set[s];
+          ++f;
+        }
+    }
+  } catch (const std::exception& e) {
+    goal::set_last_error(e.what());
+    return GOAL_ERR_STATE;
+  }
+  return GOAL_OK;
+}
+
+int goal_coarsener_destroy(goal_coarsener h) {
+  delete h;
+  return GOAL_OK;
+}
+
+}  // extern "C"

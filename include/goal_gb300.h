@@ -133,6 +133,33 @@ int goal_refiner_get(goal_refiner r, double* coords, int* node_parents, int* tet
                      int* tri_set);
 int goal_refiner_destroy(goal_refiner r);
 
+/* Coarsening to the target size by edge collapse, the other half of the
+ * adaptation loop (same reference site; ma::adapt coarsens as well as
+ * refines). An edge (a, b) shorter than ratio x (mean target size of its end
+ * points) is collapsed by moving b onto a if node_class[b] has no bit that
+ * node_class[a] lacks (the caller's node / side set memberships; the boundary
+ * is added here), b is not on an element-set interface, a boundary b sits on a
+ * flat part of the boundary and (a, b) is a boundary edge, the link condition
+ * holds, every tet left around b stays positively oriented with mean-ratio
+ * quality >= min(min_quality, the worst quality around b before), and no new
+ * edge is longer than refine_ratio x its mean target size. Shortest (relative)
+ * edges first, one independent set of collapses per pass, up to max_passes.
+ * create: the mesh (elem_set may be NULL), node_class[num_nodes], side
+ * triangles; coarsen: vtx_size[num_nodes] -> sizes[0..2] = nodes, elements,
+ * side triangles left; get: coords[3*nodes], node_origin[nodes] (original node
+ * of each kept node, in original order), tets[4*elements],
+ * elem_origin[elements] (original element of each tet), tris/tri_set (may be
+ * NULL). */
+typedef struct goal_coarsener_s* goal_coarsener;
+int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, const int* tets, const int* elem_set,
+                          const long long* node_class, int num_sides, const int* tris, const int* tri_set,
+                          goal_coarsener* out);
+int goal_coarsener_coarsen(goal_coarsener c, const double* vtx_size, double ratio, double refine_ratio,
+                           double min_quality, int max_passes, long long* sizes);
+int goal_coarsener_get(goal_coarsener c, double* coords, int* node_origin, int* tets, int* elem_origin, int* tris,
+                       int* tri_set);
+int goal_coarsener_destroy(goal_coarsener c);
+
 /* ---------------------------------------------------------------- Mechanics
  * goal::create_mechanics (src/goal_mechanics.hpp:50). materials holds, per
  * element set, E, nu, K, Y, c0 (K and Y are read by J2 only). States start as
