@@ -346,4 +346,40 @@ inline RefinedMesh refine_to_size(const std::vector<double>& coords, const std::
   return m;
 }
 
+// Coarsening to the target size (goal_coarsener_*): node_class holds the
+// caller's set memberships per node (a collapsed node's sets must be a subset
+// of its target's); elem_set may be empty (one set).
+struct CoarsenedMesh {
+  std::vector<double> coords;
+  std::vector<int> tets, elem_origin, node_origin, tris, tri_set;
+};
+inline CoarsenedMesh coarsen_to_size(const std::vector<double>& coords, const std::vector<int>& tets,
+                                     const std::vector<int>& elem_set, const std::vector<long long>& node_class,
+                                     const std::vector<int>& tris, const std::vector<int>& tri_set,
+                                     const std::vector<double>& vtx_size, double ratio = 0.5,
+                                     double refine_ratio = 1.5, double min_quality = 0.2, int max_passes = 8) {
+  goal_coarsener c = nullptr;
+  check(goal_coarsener_create((int)(coords.size() / 3), coords.data(), (int)(tets.size() / 4), tets.data(),
+                              elem_set.empty() ? nullptr : elem_set.data(), node_class.data(), (int)tri_set.size(),
+                              tris.data(), tri_set.data(), &c));
+  long long sizes[3];
+  int rc = goal_coarsener_coarsen(c, vtx_size.data(), ratio, refine_ratio, min_quality, max_passes, sizes);
+  if (rc != GOAL_OK) {
+    goal_coarsener_destroy(c);
+    check(rc);
+  }
+  CoarsenedMesh m;
+  m.coords.resize(3 * sizes[0]);
+  m.node_origin.resize(sizes[0]);
+  m.tets.resize(4 * sizes[1]);
+  m.elem_origin.resize(sizes[1]);
+  m.tris.resize(3 * sizes[2]);
+  m.tri_set.resize(sizes[2]);
+  rc = goal_coarsener_get(c, m.coords.data(), m.node_origin.data(), m.tets.data(), m.elem_origin.data(),
+                          m.tris.data(), m.tri_set.data());
+  goal_coarsener_destroy(c);
+  check(rc);
+  return m;
+}
+
 }  // namespace goal

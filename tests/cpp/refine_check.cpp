@@ -1,7 +1,9 @@
 // C++ through goal.hpp: refines a 2x2x2 Kuhn cube near one corner with
 // goal::refine_to_size (the C ABI's host refiner) and checks that the refined
 // tets tile the unit cube (total volume 1, every volume positive) and that
-// every new node sits at the midpoint of its parent edge. Runs without a GPU.
+// every new node sits at the midpoint of its parent edge; then coarsens the
+// result with goal::coarsen_to_size and checks the tiling again. Runs without
+// a GPU.
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -63,5 +65,21 @@ int main() {
   std::printf("refined %zu -> %zu tets, volume %.17g, min %.3g, midpoint error %.3g\n", T.size() / 4,
               m.tets.size() / 4, total, vmin, mid_err);
   const bool ok = m.tets.size() > T.size() && std::fabs(total - 1.0) < 1e-13 && vmin > 0.0 && mid_err == 0.0;
-  return ok ? 0 : 1;
+  // and back: goal::coarsen_to_size with a uniform size of half the cube (no
+  // sets: the box's corners and edges are kept because their boundary faces
+  // are not coplanar)
+  std::vector<double> big(X.size() / 3, 0.5);
+  std::vector<long long> cls(X.size() / 3, 0);
+  goal::CoarsenedMesh c = goal::coarsen_to_size(X, m.tets, {}, cls, {}, {}, big);
+  X = c.coords;
+  double ctotal = 0.0, cmin = 1.0;
+  for (size_t e = 0; e < c.tets.size() / 4; ++e) {
+    const double v = vol(&c.tets[4 * e]);
+    ctotal += v;
+    cmin = std::fmin(cmin, v);
+  }
+  std::printf("coarsened %zu -> %zu tets, volume %.17g, min %.3g\n", m.tets.size() / 4, c.tets.size() / 4, ctotal,
+              cmin);
+  const bool ok2 = c.tets.size() < m.tets.size() && std::fabs(ctotal - 1.0) < 1e-13 && cmin > 0.0;
+  return ok && ok2 ? 0 : 1;
 }
