@@ -133,6 +133,44 @@ def coarsen_to_size(mesh: Mesh, vtx_size: np.ndarray, ratio: float = 0.5, refine
     return out, org_n, org_e
 
 
+def improve_shape(mesh: Mesh, target_quality: float = 0.3, max_passes: int = 4) -> Tuple[Mesh, np.ndarray]:
+    """Flips (3-2 and 2-3, nodes fixed) around tets of mean-ratio quality
+    below ``target_quality`` (``goal_coarsener_swap``). Returns the improved
+    mesh and the original element of each element (the old tet that holds the
+    new tet's centroid)."""
+    L = lib()
+    N, E = mesh.num_nodes, mesh.num_elems
+    names = sorted(mesh.side_sets)
+    tris = [np.asarray(mesh.side_sets[k], np.int32).reshape(-1, 3) for k in names]
+    tri = np.ascontiguousarray(np.concatenate(tris) if tris else np.zeros((0, 3), np.int32), dtype=np.int32)
+    tri_set = np.ascontiguousarray(np.concatenate([np.full(len(t), i, np.int32) for i, t in enumerate(tris)])
+                                   if tris else np.zeros(0, np.int32))
+    coords = _f64(mesh.coords)
+    tets = _i32(mesh.tets)
+    eset = _i32(mesh.elem_set)
+    cls = np.ascontiguousarray(_node_class(mesh))
+    h = ctypes.c_void_p()
+    check(L.goal_coarsener_create(N, _ptr(coords), E, _ptr(tets), _ptr(eset), _ptr(cls), len(tri), _ptr(tri),
+                                  _ptr(tri_set), ctypes.byref(h)))
+    try:
+        sizes = (ctypes.c_longlong * 3)()
+        check(L.goal_coarsener_swap(h, float(target_quality), int(max_passes), sizes))
+        n2, e2, s2 = int(sizes[0]), int(sizes[1]), int(sizes[2])
+        X = np.zeros((n2, 3))
+        org_n = np.zeros(n2, np.int32)
+        T = np.zeros((e2, 4), np.int32)
+        org_e = np.zeros(e2, np.int32)
+        tri2 = np.zeros((s2, 3), np.int32)
+        tset2 = np.zeros(s2, np.int32)
+        check(L.goal_coarsener_get(h, _ptr(X), _ptr(org_n), _ptr(T), _ptr(org_e), _ptr(tri2), _ptr(tset2)))
+    finally:
+        L.goal_coarsener_destroy(h)
+    side_sets = {name: tri2[tset2 == i] for i, name in enumerate(names)}
+    out = Mesh(coords=X, tets=T, elem_set=np.asarray(mesh.elem_set)[org_e].astype(np.int32),
+               elem_set_names=list(mesh.elem_set_names), node_sets=dict(mesh.node_sets), side_sets=side_sets)
+    return out, org_e
+
+
 class Transfer:
     """Moves nodal fields and element states from the mesh before an
     adaptation to the mesh after it: through the coarsening (kept nodes keep
@@ -160,13 +198,19 @@ class Transfer:
 
 
 def adapt_to_size(mesh: Mesh, vtx_size: np.ndarray, coarsen_ratio: float = 0.5, refine_ratio: float = 1.5,
-                  min_quality: float = 0.2, max_elems: int = 50_000_000) -> Tuple[Mesh, Transfer]:
+                  min_quality: float = 0.2, max_elems: int = 50_000_000,
+                  improve_quality: float = 0.0) -> Tuple[Mesh, Transfer]:
     """One adaptation to a size field: coarsen (edges shorter than
-    coarsen_ratio x size), then refine (edges longer than refine_ratio x
-    size). Returns the adapted mesh and the transfer of fields onto it."""
+    coarsen_ratio x size), optionally flip around tets of quality below
+    improve_quality (0: no flips), then refine (edges longer than
+    refine_ratio x size). Returns the adapted mesh and the transfer of fields
+    onto it."""
     size = _f64(vtx_size)
     mc, org_n, org_ec = coarsen_to_size(mesh, size, ratio=coarsen_ratio, refine_ratio=refine_ratio,
                                         min_quality=min_quality)
+    if improve_quality > 0.0:
+        mc, org_f = improve_shape(mc, target_quality=improve_quality)
+        org_ec = np.asarray(org_ec)[org_f]
     mr, parents, org_er = refine_to_size(mc, size[org_n], ratio=refine_ratio, max_elems=max_elems)
     return mr, Transfer(org_n, org_ec, parents, org_er)
 

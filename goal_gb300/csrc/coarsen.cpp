@@ -46,6 +46,7 @@ struct Coarsener {
   std::vector<char> valive;
   std::vector<std::array<int, 4>> T;
   std::vector<int> eset;
+  std::vector<int> origin;  // original element of each tet (swaps make new ones)
   std::vector<char> talive;
   std::vector<std::vector<int>> vt;  // vertex -> tets (live ones; dead entries are filtered on use)
   // boundary faces (faces of exactly one tet) and side triangles
@@ -268,6 +269,189 @@ struct Coarsener {
     compact(vs[a], salive);
   }
 
+  // ----- shape improvement by flips (nodes fixed) -----
+  // tets around edge (d, e)
+  void edge_tets(int d, int e, std::vector<int>& out) const {
+    out.clear();
+    for (int t : vt[d])
+      if (talive[t] && has(T[t], e)) out.push_back(t);
+  }
+  bool boundary_edge(int d, int e) const {
+    for (int f : vf[d])
+      if (falive[f] && has3(F[f], e)) return true;
+    return false;
+  }
+  bool side_edge(int d, int e) const {
+    for (int f : vs[d])
+      if (salive[f] && has3(S[f], e)) return true;
+    return false;
+  }
+  bool side_face(int a, int b, int c) const {
+    for (int f : vs[a])
+      if (salive[f] && has3(S[f], b) && has3(S[f], c)) return true;
+    return false;
+  }
+  // the tet across face (a, b, c) of t, or -1
+  int across(int t, int a, int b, int c) const {
+    for (int u : vt[a])
+      if (u != t && talive[u] && has(T[u], b) && has(T[u], c)) return u;
+    return -1;
+  }
+  std::array<int, 4> oriented(int a, int b, int c, int d) const {
+    std::array<int, 4> v = {a, b, c, d};
+    if (vol6(v) < 0.0) std::swap(v[2], v[3]);
+    return v;
+  }
+  // the old tet (of ts) that contains the centroid of v best
+  int donor(const std::array<int, 4>& v, const std::vector<int>& ts) const {
+    double cen[3] = {0, 0, 0};
+    for (int x : v)
+      for (int c = 0; c < 3; ++c) cen[c] += 0.25 * X[3 * x + c];
+    int best = ts[0];
+    double best_b = -1e300;
+    for (int t : ts) {
+      // barycentric coordinates of cen in T[t]: the smallest one
+      const auto& w = T[t];
+      const double V = vol6(w);
+      double bmin = 1e300;
+      for (int k = 0; k < 4; ++k) {
+        std::array<double, 12> P;
+        for (int q = 0; q < 4; ++q)
+          for (int c = 0; c < 3; ++c) P[3 * q + c] = (q == k) ? cen[c] : X[3 * w[q] + c];
+        double e[3][3];
+        for (int q = 0; q < 3; ++q)
+          for (int c = 0; c < 3; ++c) e[q][c] = P[3 * (q + 1) + c] - P[c];
+        const double vk = e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) -
+                          e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+                          e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+        bmin = std::min(bmin, vk / V);
+      }
+      if (bmin > best_b) { best_b = bmin; best = t; }
+    }
+    return best;
+  }
+  void replace(const std::vector<int>& old, const std::vector<std::array<int, 4>>& nu) {
+    std::vector<int> org;
+    for (const auto& v : nu) org.push_back(origin[donor(v, old)]);
+    const int es = eset[old[0]];
+    for (int t : old) talive[t] = 0;
+    for (size_t k = 0; k < nu.size(); ++k) {
+      const int id = (int)T.size();
+      T.push_back(nu[k]);
+      eset.push_back(es);
+      origin.push_back(org[k]);
+      talive.push_back(1);
+      for (int x : nu[k]) vt[x].push_back(id);
+    }
+    for (const auto& v : nu)
+      for (int x : v) compact(vt[x], talive);
+  }
+  // best flip touching tet t; returns the new min quality (0: none found)
+  double best_flip(int t, std::vector<int>& old, std::vector<std::array<int, 4>>& nu) const {
+    const double q0 = quality(T[t]);
+    double best = q0 * (1.0 + 1e-3);
+    bool found = false;
+    std::vector<int> ring;
+    const auto v = T[t];
+    // 3-2: an interior edge with three tets around it
+    for (int i = 0; i < 4; ++i)
+      for (int j = i + 1; j < 4; ++j) {
+        const int d = v[i], e = v[j];
+        if (boundary_edge(d, e) || side_edge(d, e)) continue;
+        edge_tets(d, e, ring);
+        if (ring.size() != 3) continue;
+        if (eset[ring[0]] != eset[ring[1]] || eset[ring[0]] != eset[ring[2]]) continue;
+        std::vector<int> oth;
+        double qold = 1.0;
+        for (int u : ring) {
+          qold = std::min(qold, quality(T[u]));
+          for (int x : T[u])
+            if (x != d && x != e) oth.push_back(x);
+        }
+        std::sort(oth.begin(), oth.end());
+        oth.erase(std::unique(oth.begin(), oth.end()), oth.end());
+        if (oth.size() != 3) continue;
+        const int a = oth[0], b = oth[1], c = oth[2];
+        // the new face must not exist already
+        bool exists = false;
+        for (int u : vt[a])
+          if (talive[u] && has(T[u], b) && has(T[u], c) && std::find(ring.begin(), ring.end(), u) == ring.end())
+            exists = true;
+        if (exists) continue;
+        // d-e must cross the triangle abc's interior (then the two new tets
+        // fill exactly the three old ones)
+        const std::array<int, 4> s1 = {a, b, d, e}, s2 = {b, c, d, e}, s3 = {c, a, d, e};
+        const double v1 = vol6(s1), v2 = vol6(s2), v3 = vol6(s3);
+        if (!((v1 > 0 && v2 > 0 && v3 > 0) || (v1 < 0 && v2 < 0 && v3 < 0))) continue;
+        const auto n1 = oriented(a, b, c, d), n2 = oriented(a, b, c, e);
+        if (!(vol6(n1) > 0.0) || !(vol6(n2) > 0.0)) continue;
+        const double qn = std::min(quality(n1), quality(n2));
+        if (qn > best && qn > qold) {
+          best = qn;
+          old = ring;
+          nu = {n1, n2};
+          found = true;
+        }
+      }
+    // 2-3: an interior face shared with a tet of the same set
+    static const int kF[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
+    for (int k = 0; k < 4; ++k) {
+      const int a = v[kF[k][0]], b = v[kF[k][1]], c = v[kF[k][2]], d = v[k];
+      if (side_face(a, b, c)) continue;
+      const int u = across(t, a, b, c);
+      if (u < 0 || eset[u] != eset[t]) continue;
+      int e = -1;
+      for (int x : T[u])
+        if (x != a && x != b && x != c) e = x;
+      if (e < 0 || e == d) continue;
+      // the new edge (d, e) must not exist already
+      bool exists = false;
+      for (int w : vt[d])
+        if (talive[w] && has(T[w], e)) exists = true;
+      if (exists) continue;
+      const std::array<int, 4> s1 = {a, b, d, e}, s2 = {b, c, d, e}, s3 = {c, a, d, e};
+      const double v1 = vol6(s1), v2 = vol6(s2), v3 = vol6(s3);
+      // d-e crosses the face's interior: the three have one strict sign
+      if (!((v1 > 0 && v2 > 0 && v3 > 0) || (v1 < 0 && v2 < 0 && v3 < 0))) continue;
+      const auto n1 = oriented(a, b, d, e), n2 = oriented(b, c, d, e), n3 = oriented(c, a, d, e);
+      const double qold = std::min(q0, quality(T[u]));
+      const double qn = std::min(quality(n1), std::min(quality(n2), quality(n3)));
+      if (qn > best && qn > qold) {
+        best = qn;
+        old = {t, u};
+        nu = {n1, n2, n3};
+        found = true;
+      }
+    }
+    return found ? best : 0.0;
+  }
+  int swap_pass(double target_quality) {
+    std::vector<std::pair<double, int>> bad;
+    for (size_t t = 0; t < T.size(); ++t)
+      if (talive[t]) {
+        const double q = quality(T[t]);
+        if (q < target_quality) bad.push_back({q, (int)t});
+      }
+    std::sort(bad.begin(), bad.end());
+    std::vector<char> touched(N, 0);
+    std::vector<int> old;
+    std::vector<std::array<int, 4>> nu;
+    int done = 0;
+    for (const auto& qt : bad) {
+      const int t = qt.second;
+      if (!talive[t]) continue;
+      bool skip = false;
+      for (int x : T[t]) skip |= touched[x] != 0;
+      if (skip) continue;
+      if (best_flip(t, old, nu) <= 0.0) continue;
+      for (int u : old)
+        for (int x : T[u]) touched[x] = 1;
+      replace(old, nu);
+      ++done;
+    }
+    return done;
+  }
+
   int pass(double ratio, double refine_ratio, double min_quality) {
     struct Cand {
       double r;
@@ -360,6 +544,7 @@ int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, co
         c.vt[v].push_back(e);
       }
       c.eset[e] = elem_set ? elem_set[e] : 0;
+      c.origin.push_back(e);
       for (auto& fq : kFaces) {
         std::array<int, 3> f = {c.T[e][fq[0]], c.T[e][fq[1]], c.T[e][fq[2]]};
         std::array<int, 3> sf = f;
@@ -441,6 +626,30 @@ int goal_coarsener_coarsen(goal_coarsener h, const double* vtx_size, double rati
   return GOAL_OK;
 }
 
+int goal_coarsener_swap(goal_coarsener h, double target_quality, int max_passes, long long* sizes) {
+  try {
+    if (!h || !sizes || !(target_quality > 0.0) || target_quality > 1.0)
+      throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_swap: bad arguments");
+    goal::Coarsener& c = h->c;
+    for (int p = 0; p < max_passes; ++p)
+      if (c.swap_pass(target_quality) == 0) break;
+    long long nn = 0, ne = 0, ns = 0;
+    for (char a : c.valive) nn += a ? 1 : 0;
+    for (char a : c.talive) ne += a ? 1 : 0;
+    for (char a : c.salive) ns += a ? 1 : 0;
+    sizes[0] = nn;
+    sizes[1] = ne;
+    sizes[2] = ns;
+  } catch (const goal::Error& e) {
+    goal::set_last_error(e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    goal::set_last_error(e.what());
+    return GOAL_ERR_STATE;
+  }
+  return GOAL_OK;
+}
+
 int goal_coarsener_get(goal_coarsener h, double* coords, int* node_origin, int* tets, int* elem_origin, int* tris,
                        int* tri_set) {
   try {
@@ -460,7 +669,7 @@ int goal_coarsener_get(goal_coarsener h, double* coords, int* node_origin, int* 
     for (size_t t = 0; t < c.T.size(); ++t)
       if (c.talive[t]) {
         for (int q = 0; q < 4; ++q) tets[4 * e + q] = renum[c.T[t][q]];
-        elem_origin[e] = (int)t;
+        elem_origin[e] = c.origin[t];
         ++e;
       }
     if (tris && tri_set) {

@@ -156,6 +156,14 @@ int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, co
                           goal_coarsener* out);
 int goal_coarsener_coarsen(goal_coarsener c, const double* vtx_size, double ratio, double refine_ratio,
                            double min_quality, int max_passes, long long* sizes);
+/* Shape improvement by flips, nodes fixed (ma::adapt's shape correction in
+ * part): tets with mean-ratio quality below target_quality, worst first, try
+ * the 3-2 flip of each interior edge with three tets around it and the 2-3
+ * flip of each interior face; the flip that raises the local minimum quality
+ * most is taken. Flips stay inside one element set and do not cross side
+ * triangles. A new tet takes the original element of the old tet that holds
+ * its centroid. sizes as for coarsen. Callable with or without coarsen. */
+int goal_coarsener_swap(goal_coarsener c, double target_quality, int max_passes, long long* sizes);
 int goal_coarsener_get(goal_coarsener c, double* coords, int* node_origin, int* tets, int* elem_origin, int* tris,
                        int* tri_set);
 int goal_coarsener_destroy(goal_coarsener c);

@@ -1,9 +1,10 @@
 """Coarsening by edge collapse (the coarsening half of goal's adaptation
-step) and the coarsen-then-refine adaptation with its field transfer. Host
-code, run on the CPU: conformity, positive orientation, volume (per element
-set) and boundary area preserved, boundary nodes and side sets kept on their
-planes, the length and quality bounds, determinism, and exact transfer of a
-linear field."""
+step), shape improvement by 2-3 / 3-2 flips, and the coarsen-then-refine
+adaptation with its field transfer. Host code, run on the CPU: conformity,
+positive orientation, volume (per element set) and boundary area preserved,
+boundary nodes and side sets kept on their planes, the length and quality
+bounds, flips that pick the better of the two bipyramid configurations,
+determinism, and exact transfer of a linear field."""
 import numpy as np
 
 from goal_gb300 import adapt
@@ -116,3 +117,53 @@ def test_nothing_to_collapse_is_identity():
     assert np.array_equal(out.tets, mesh.tets) and np.array_equal(out.coords, mesh.coords)
     assert np.array_equal(node_origin, np.arange(mesh.num_nodes))
     assert np.array_equal(elem_origin, np.arange(mesh.num_elems))
+
+
+def _bipyramid(h, ring):
+    """Triangle a b c on the unit circle (z = 0) and apexes d, e = (0, 0, -/+h):
+    the two tets across face abc, or the three tets around edge de."""
+    from goal_gb300.mesh import Mesh
+    ang = np.array([0.0, 2.0, 4.0]) * np.pi / 3.0
+    X = np.array([[np.cos(t), np.sin(t), 0.0] for t in ang] + [[0.0, 0.0, -h], [0.0, 0.0, h]])
+    T = np.array([[0, 1, 3, 4], [1, 2, 3, 4], [2, 0, 3, 4]] if ring else [[0, 1, 2, 3], [0, 1, 2, 4]], np.int32)
+    m = Mesh(coords=X, tets=T, elem_set=np.zeros(len(T), np.int32), elem_set_names=["b"], node_sets={},
+             side_sets={})
+    v = _volumes(m)
+    m.tets[v < 0] = m.tets[v < 0][:, [0, 1, 3, 2]]
+    return m
+
+
+def test_flips_take_the_better_configuration():
+    # flat bipyramid: three tets around the short axis beat two across the face
+    m = _bipyramid(0.2, ring=False)
+    out, origin = adapt.improve_shape(m, target_quality=0.6)
+    assert out.num_elems == 3 and _volumes(out).min() > 0
+    assert abs(_volumes(out).sum() - _volumes(m).sum()) < 1e-14
+    assert _quality(out).min() > _quality(m).min() + 0.1
+    assert set(origin) <= {0, 1}
+    # tall bipyramid: two tets across the face beat the three around the axis
+    m = _bipyramid(2.0, ring=True)
+    out, origin = adapt.improve_shape(m, target_quality=0.6)
+    assert out.num_elems == 2 and _volumes(out).min() > 0
+    assert abs(_volumes(out).sum() - _volumes(m).sum()) < 1e-14
+    assert _quality(out).min() > 0.9
+    # good enough already: untouched
+    m = _bipyramid(1.2, ring=False)
+    out, origin = adapt.improve_shape(m, target_quality=0.6)
+    assert np.array_equal(out.tets, m.tets) and np.array_equal(origin, [0, 1])
+
+
+def test_flips_after_coarsening_keep_the_mesh_valid():
+    mesh = kuhn_cube(10)
+    mc, _, _ = adapt.coarsen_to_size(mesh, np.full(mesh.num_nodes, 0.35))
+    out, origin = adapt.improve_shape(mc, target_quality=0.4)
+    bnd = {tuple(f) for f in _check_conforming(out)}
+    v = _volumes(out)
+    assert v.min() > 0 and abs(v.sum() - 1.0) < 1e-12
+    q0, q1 = _quality(mc), _quality(out)
+    assert q1.min() >= q0.min() - 1e-12
+    assert np.percentile(q1, 5) >= np.percentile(q0, 5) - 1e-12
+    for name, (d, val) in PLANES.items():
+        assert abs(_area(out.coords, out.side_sets[name]) - 1.0) < 1e-12
+        assert all(tuple(sorted(t)) in bnd for t in out.side_sets[name])
+    assert origin.min() >= 0 and origin.max() < mc.num_elems
