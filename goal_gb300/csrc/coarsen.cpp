@@ -139,17 +139,36 @@ struct Coarsener {
       }
       if (!edge_on_boundary) return false;
     }
+    thread_local std::vector<int> adj_a, adj_b, common, lab;
+    thread_local std::vector<uint64_t> elab, ea, eb;
+    adjacent(b, adj_b);
+    if (!std::binary_search(adj_b.begin(), adj_b.end(), a)) return false;
+    // geometry: the tets that keep b (as a) stay valid and good enough; no
+    // new edge too long
+    double worst = 1.0;
+    for (int t : vt[b])
+      if (talive[t]) worst = std::min(worst, quality(T[t]));
+    const double qmin = std::min(min_quality, worst);
+    for (int t : vt[b]) {
+      if (!talive[t] || has(T[t], a)) continue;
+      std::array<int, 4> v = T[t];
+      for (int& x : v)
+        if (x == b) x = a;
+      if (!(vol6(v) > 0.0) || quality(v) < qmin) return false;
+    }
+    for (int c : adj_b) {
+      if (c == a) continue;
+      const double s = refine_ratio * 0.5 * (size[a] + size[c]);
+      if (len2(a, c) > s * s) return false;
+    }
     // link condition: the vertices adjacent to both a and b are exactly the
     // vertices of the tets around edge ab; edges (c, d) seen from both a and b
     // must belong to a tet around ab
-    std::vector<int> adj_a, adj_b;
     adjacent(a, adj_a);
-    adjacent(b, adj_b);
-    if (!std::binary_search(adj_b.begin(), adj_b.end(), a)) return false;
-    std::vector<int> common;
+    common.clear();
     std::set_intersection(adj_a.begin(), adj_a.end(), adj_b.begin(), adj_b.end(), std::back_inserter(common));
-    std::vector<int> lab;
-    std::unordered_set<uint64_t> elab;
+    lab.clear();
+    elab.clear();
     for (int t : vt[b]) {
       if (!talive[t] || !has(T[t], a)) continue;
       int cd[2], k = 0;
@@ -157,30 +176,44 @@ struct Coarsener {
         if (x != a && x != b) cd[k++] = x;
       lab.push_back(cd[0]);
       lab.push_back(cd[1]);
-      elab.insert(ekey(cd[0], cd[1]));
+      elab.push_back(ekey(cd[0], cd[1]));
     }
     std::sort(lab.begin(), lab.end());
     lab.erase(std::unique(lab.begin(), lab.end()), lab.end());
     if (common != lab) return false;
     {
-      std::unordered_set<uint64_t> ea;
+      std::sort(elab.begin(), elab.end());
+      ea.clear();
+      eb.clear();
       for (int t : vt[a]) {
         if (!talive[t] || has(T[t], b)) continue;
         int cd[3], k = 0;
         for (int x : T[t])
           if (x != a) cd[k++] = x;
-        ea.insert(ekey(cd[0], cd[1]));
-        ea.insert(ekey(cd[0], cd[2]));
-        ea.insert(ekey(cd[1], cd[2]));
+        ea.push_back(ekey(cd[0], cd[1]));
+        ea.push_back(ekey(cd[0], cd[2]));
+        ea.push_back(ekey(cd[1], cd[2]));
       }
       for (int t : vt[b]) {
         if (!talive[t] || has(T[t], a)) continue;
         int cd[3], k = 0;
         for (int x : T[t])
           if (x != b) cd[k++] = x;
-        const uint64_t e3[3] = {ekey(cd[0], cd[1]), ekey(cd[0], cd[2]), ekey(cd[1], cd[2])};
-        for (uint64_t e : e3)
-          if (ea.count(e) && !elab.count(e)) return false;
+        eb.push_back(ekey(cd[0], cd[1]));
+        eb.push_back(ekey(cd[0], cd[2]));
+        eb.push_back(ekey(cd[1], cd[2]));
+      }
+      std::sort(ea.begin(), ea.end());
+      std::sort(eb.begin(), eb.end());
+      size_t i = 0, j = 0;
+      while (i < ea.size() && j < eb.size()) {
+        if (ea[i] < eb[j]) ++i;
+        else if (eb[j] < ea[i]) ++j;
+        else {
+          if (!std::binary_search(elab.begin(), elab.end(), ea[i])) return false;
+          ++i;
+          ++j;
+        }
       }
     }
     // the same on the boundary surface: a boundary vertex c joined to both a
@@ -207,24 +240,6 @@ struct Coarsener {
       std::set_intersection(ca.begin(), ca.end(), cb.begin(), cb.end(), std::back_inserter(both));
       for (int c : both)
         if (std::find(fab.begin(), fab.end(), c) == fab.end()) return false;
-    }
-    // geometry: the tets that keep b (as a) stay valid and good enough; no
-    // new edge too long
-    double worst = 1.0;
-    for (int t : vt[b])
-      if (talive[t]) worst = std::min(worst, quality(T[t]));
-    const double qmin = std::min(min_quality, worst);
-    for (int t : vt[b]) {
-      if (!talive[t] || has(T[t], a)) continue;
-      std::array<int, 4> v = T[t];
-      for (int& x : v)
-        if (x == b) x = a;
-      if (!(vol6(v) > 0.0) || quality(v) < qmin) return false;
-    }
-    for (int c : adj_b) {
-      if (c == a) continue;
-      const double s = refine_ratio * 0.5 * (size[a] + size[c]);
-      if (len2(a, c) > s * s) return false;
     }
     return true;
   }
@@ -458,18 +473,21 @@ struct Coarsener {
       uint64_t key;
     };
     std::vector<Cand> cand;
-    std::unordered_set<uint64_t> seen;
+    std::vector<uint64_t> keys;
+    keys.reserve(6 * T.size());
     for (size_t t = 0; t < T.size(); ++t) {
       if (!talive[t]) continue;
       const auto& v = T[t];
       for (int i = 0; i < 4; ++i)
-        for (int j = i + 1; j < 4; ++j) {
-          const uint64_t k = ekey(v[i], v[j]);
-          if (!seen.insert(k).second) continue;
-          const double s = 0.5 * (size[v[i]] + size[v[j]]);
-          const double r = std::sqrt(len2(v[i], v[j])) / s;
-          if (r < ratio) cand.push_back({r, k});
-        }
+        for (int j = i + 1; j < 4; ++j) keys.push_back(ekey(v[i], v[j]));
+    }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    for (uint64_t k : keys) {
+      const int lo = (int)(k & 0xffffffffu), hi = (int)(k >> 32);
+      const double s = 0.5 * (size[lo] + size[hi]);
+      const double r = std::sqrt(len2(lo, hi)) / s;
+      if (r < ratio) cand.push_back({r, k});
     }
     std::sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) {
       return x.r != y.r ? x.r < y.r : x.key < y.key;
@@ -524,18 +542,15 @@ int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, co
     c.vt.assign(num_nodes, {});
     c.vf.assign(num_nodes, {});
     c.vs.assign(num_nodes, {});
-    // boundary faces: the faces of exactly one tet
-    struct FaceRec {
-      std::array<int, 3> v;
-      int count;
-    };
-    std::unordered_map<uint64_t, std::vector<FaceRec>> faces;
-    auto fkey = [](std::array<int, 3> s) {
-      std::sort(s.begin(), s.end());
-      return ((uint64_t)(unsigned)s[0] * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)(unsigned)s[1] << 21) ^
-             ((uint64_t)(unsigned)s[2] << 42) ^ (uint64_t)(unsigned)s[2];
-    };
+    // boundary faces: the faces of exactly one tet (sorted vertex triples,
+    // sorted, counted by runs)
     static const int kFaces[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
+    struct FaceRec {
+      std::array<int, 3> key;  // sorted vertices
+      std::array<int, 3> v;    // as in the tet
+    };
+    std::vector<FaceRec> all;
+    all.reserve(4ull * num_elems);
     for (int e = 0; e < num_elems; ++e) {
       for (int q = 0; q < 4; ++q) {
         const int v = tets[4ll * e + q];
@@ -546,27 +561,21 @@ int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, co
       c.eset[e] = elem_set ? elem_set[e] : 0;
       c.origin.push_back(e);
       for (auto& fq : kFaces) {
-        std::array<int, 3> f = {c.T[e][fq[0]], c.T[e][fq[1]], c.T[e][fq[2]]};
-        std::array<int, 3> sf = f;
-        std::sort(sf.begin(), sf.end());
-        auto& bucket = faces[fkey(f)];
-        bool found = false;
-        for (auto& r : bucket) {
-          std::array<int, 3> sr = r.v;
-          std::sort(sr.begin(), sr.end());
-          if (sr == sf) {
-            ++r.count;
-            found = true;
-            break;
-          }
-        }
-        if (!found) bucket.push_back({f, 1});
+        FaceRec r;
+        r.v = {c.T[e][fq[0]], c.T[e][fq[1]], c.T[e][fq[2]]};
+        r.key = r.v;
+        std::sort(r.key.begin(), r.key.end());
+        all.push_back(r);
       }
     }
+    std::sort(all.begin(), all.end(), [](const FaceRec& x, const FaceRec& y) { return x.key < y.key; });
     std::vector<std::array<int, 3>> bfaces;
-    for (auto& kv : faces)
-      for (auto& r : kv.second)
-        if (r.count == 1) bfaces.push_back(r.v);
+    for (size_t i = 0; i < all.size();) {
+      size_t j = i + 1;
+      while (j < all.size() && all[j].key == all[i].key) ++j;
+      if (j - i == 1) bfaces.push_back(all[i].v);
+      i = j;
+    }
     std::sort(bfaces.begin(), bfaces.end());  // deterministic order
     for (const auto& f : bfaces) {
       const int id = (int)c.F.size();
