@@ -21,8 +21,6 @@
 #include <cmath>
 #include <cstdint>
 #include <memory>
-#include <unordered_map>
-#include <unordered_set>
 #include <vector>
 
 #include "../../include/goal_gb300.h"
