@@ -14,7 +14,6 @@
 #include <cstdint>
 #include <memory>
 #include <stdexcept>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/goal_gb300.h"
@@ -30,6 +29,95 @@ inline uint64_t edge_key(int a, int b) {
 
 constexpr int kEdges[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 
+// Open-addressing map from an edge key (never 0: the end points differ) to a
+// dense id, with linear probing; keys are never removed.
+struct EdgeIds {
+  std::vector<uint64_t> keys;
+  std::vector<int> ids;
+  size_t count = 0;
+  EdgeIds() { rehash(1 << 16); }
+  static size_t hash(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    return (size_t)k;
+  }
+  void rehash(size_t cap) {
+    std::vector<uint64_t> ok = std::move(keys);
+    std::vector<int> oi = std::move(ids);
+    keys.assign(cap, 0);
+    ids.assign(cap, -1);
+    for (size_t i = 0; i < ok.size(); ++i)
+      if (ok[i]) {
+        size_t h = hash(ok[i]) & (cap - 1);
+        while (keys[h]) h = (h + 1) & (cap - 1);
+        keys[h] = ok[i];
+        ids[h] = oi[i];
+      }
+  }
+  int find(uint64_t k) const {
+    const size_t mask = keys.size() - 1;
+    for (size_t h = hash(k) & mask;; h = (h + 1) & mask) {
+      if (keys[h] == k) return ids[h];
+      if (!keys[h]) return -1;
+    }
+  }
+  // the id of k, inserting next_id when absent (inserted set accordingly)
+  int get(uint64_t k, int next_id, bool& inserted) {
+    if (2 * (count + 1) > keys.size()) rehash(2 * keys.size());
+    const size_t mask = keys.size() - 1;
+    for (size_t h = hash(k) & mask;; h = (h + 1) & mask) {
+      if (keys[h] == k) {
+        inserted = false;
+        return ids[h];
+      }
+      if (!keys[h]) {
+        keys[h] = k;
+        ids[h] = next_id;
+        ++count;
+        inserted = true;
+        return next_id;
+      }
+    }
+  }
+};
+
+// An ordered list of element ids with inline room for eight (the tets around
+// an edge of a tet mesh, or the triangles around a boundary edge)
+struct IdList {
+  int n = 0;
+  int a[8];
+  std::vector<int> more;
+  int size() const { return n; }
+  int operator[](int i) const { return i < 8 ? a[i] : more[i - 8]; }
+  void push(int v) {
+    if (n < 8) a[n] = v;
+    else more.push_back(v);
+    ++n;
+  }
+  void erase(int v) {
+    int i = 0;
+    while (i < n && (*this)[i] != v) ++i;
+    if (i == n) return;
+    for (int j = i; j + 1 < n; ++j) set(j, (*this)[j + 1]);
+    --n;
+    if (n >= 8) more.pop_back();
+  }
+  void set(int i, int v) {
+    if (i < 8) a[i] = v;
+    else more[i - 8] = v;
+  }
+  void clear() {
+    n = 0;
+    more.clear();
+  }
+  std::vector<int> copy() const {
+    std::vector<int> out(n);
+    for (int i = 0; i < n; ++i) out[i] = (*this)[i];
+    return out;
+  }
+};
+
 struct Refiner {
   std::vector<double> X;                      // 3 per node
   std::vector<double> size;                   // target size per node (new nodes: mean of the edge's)
@@ -38,13 +126,25 @@ struct Refiner {
   std::vector<int> origin;                    // original element of each tet
   std::vector<char> alive;
   long long num_alive = 0;
-  std::unordered_map<uint64_t, std::vector<int>> around;  // live tets around each edge
-  std::unordered_map<uint64_t, int> mid;                  // bisected edge -> midpoint node
+  EdgeIds edge_id;              // edge key -> dense edge id
+  std::vector<IdList> around;   // live tets around each edge (by edge id)
+  std::vector<IdList> around_s; // live side triangles around each edge
+  std::vector<int> mid;         // midpoint node of each bisected edge, -1 if none
   // side triangles (boundary faces), split with their edges
   std::vector<std::array<int, 3>> S;
   std::vector<int> S_set;
   std::vector<char> S_alive;
-  std::unordered_map<uint64_t, std::vector<int>> around_s;
+
+  int eid(uint64_t k) {
+    bool ins;
+    const int id = edge_id.get(k, (int)around.size(), ins);
+    if (ins) {
+      around.emplace_back();
+      around_s.emplace_back();
+      mid.push_back(-1);
+    }
+    return id;
+  }
 
   double len2(int a, int b) const {
     const double dx = X[3 * a] - X[3 * b], dy = X[3 * a + 1] - X[3 * b + 1], dz = X[3 * a + 2] - X[3 * b + 2];
@@ -66,37 +166,32 @@ struct Refiner {
     return edge_key(ba, bb);
   }
 
-  static void erase_from(std::vector<int>& list, int t) {
-    auto it = std::find(list.begin(), list.end(), t);
-    if (it != list.end()) list.erase(it);
-  }
   void link(int t) {
-    const auto& v = T[t];
-    for (auto& e : kEdges) around[edge_key(v[e[0]], v[e[1]])].push_back(t);
+    const auto v = T[t];
+    for (auto& e : kEdges) around[eid(edge_key(v[e[0]], v[e[1]]))].push(t);
   }
   void unlink(int t) {
-    const auto& v = T[t];
-    for (auto& e : kEdges) erase_from(around[edge_key(v[e[0]], v[e[1]])], t);
+    const auto v = T[t];
+    for (auto& e : kEdges) around[eid(edge_key(v[e[0]], v[e[1]]))].erase(t);
   }
   void link_s(int f) {
-    const auto& v = S[f];
-    for (int q = 0; q < 3; ++q) around_s[edge_key(v[q], v[(q + 1) % 3])].push_back(f);
+    const auto v = S[f];
+    for (int q = 0; q < 3; ++q) around_s[eid(edge_key(v[q], v[(q + 1) % 3]))].push(f);
   }
   void unlink_s(int f) {
-    const auto& v = S[f];
-    for (int q = 0; q < 3; ++q) erase_from(around_s[edge_key(v[q], v[(q + 1) % 3])], f);
+    const auto v = S[f];
+    for (int q = 0; q < 3; ++q) around_s[eid(edge_key(v[q], v[(q + 1) % 3]))].erase(f);
   }
 
   int midpoint(int a, int b) {
-    const uint64_t k = edge_key(a, b);
-    auto it = mid.find(k);
-    if (it != mid.end()) return it->second;
+    const int e = eid(edge_key(a, b));
+    if (mid[e] >= 0) return mid[e];
     const int m = (int)pa.size();
     for (int c = 0; c < 3; ++c) X.push_back(0.5 * (X[3 * a + c] + X[3 * b + c]));
     size.push_back(0.5 * (size[a] + size[b]));
     pa.push_back(a);
     pb.push_back(b);
-    mid.emplace(k, m);
+    mid[e] = m;
     return m;
   }
 
@@ -104,7 +199,8 @@ struct Refiner {
   void bisect(uint64_t k) {
     const int a = (int)(k & 0xffffffffu), b = (int)(k >> 32);
     const int m = midpoint(a, b);
-    const std::vector<int> tets = around[k];
+    const int ke = eid(k);
+    const std::vector<int> tets = around[ke].copy();
     for (int t : tets) {
       std::array<int, 4> v = T[t];
       int ia = -1, ib = -1;
@@ -127,10 +223,9 @@ struct Refiner {
       }
       num_alive += 1;
     }
-    around.erase(k);
-    auto its = around_s.find(k);
-    if (its != around_s.end()) {
-      const std::vector<int> tris = its->second;
+    around[ke].clear();
+    if (around_s[ke].size() > 0) {
+      const std::vector<int> tris = around_s[ke].copy();
       for (int f : tris) {
         std::array<int, 3> v = S[f];
         int ia = -1, ib = -1;
@@ -151,7 +246,7 @@ struct Refiner {
           link_s(n);
         }
       }
-      around_s.erase(k);
+      around_s[ke].clear();
     }
   }
 
@@ -160,9 +255,10 @@ struct Refiner {
     if (depth > 1000) throw Error(GOAL_ERR_STATE, "refine: longest-edge path did not end");
     while (alive[t]) {
       const uint64_t e = longest(t);
+      const IdList& ar = around[eid(e)];
       int other = -1;
-      for (int u : around[e])
-        if (longest(u) != e) { other = u; break; }
+      for (int i = 0; i < ar.size(); ++i)
+        if (longest(ar[i]) != e) { other = ar[i]; break; }
       if (other < 0) {
         bisect(e);
         return;
