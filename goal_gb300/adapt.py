@@ -171,6 +171,58 @@ def improve_shape(mesh: Mesh, target_quality: float = 0.3, max_passes: int = 4) 
     return out, org_e
 
 
+def smooth(mesh: Mesh, target_quality: float = 0.3, max_passes: int = 4) -> Tuple[Mesh, Tuple[np.ndarray, ...]]:
+    """Moves interior nodes (in no node or side set, inside one element set)
+    of low-quality stars towards the mean of their neighbours
+    (``goal_coarsener_smooth``). Returns the smoothed mesh and the nodal
+    transfer as CSR rows (ptr, ids, weights) over the input mesh's nodes: a
+    moved node takes the old field's value at its new position."""
+    L = lib()
+    N, E = mesh.num_nodes, mesh.num_elems
+    names = sorted(mesh.side_sets)
+    tris = [np.asarray(mesh.side_sets[k], np.int32).reshape(-1, 3) for k in names]
+    tri = np.ascontiguousarray(np.concatenate(tris) if tris else np.zeros((0, 3), np.int32), dtype=np.int32)
+    tri_set = np.ascontiguousarray(np.concatenate([np.full(len(t), i, np.int32) for i, t in enumerate(tris)])
+                                   if tris else np.zeros(0, np.int32))
+    coords = _f64(mesh.coords)
+    tets = _i32(mesh.tets)
+    eset = _i32(mesh.elem_set)
+    cls = np.ascontiguousarray(_node_class(mesh))
+    h = ctypes.c_void_p()
+    check(L.goal_coarsener_create(N, _ptr(coords), E, _ptr(tets), _ptr(eset), _ptr(cls), len(tri), _ptr(tri),
+                                  _ptr(tri_set), ctypes.byref(h)))
+    try:
+        nnz = ctypes.c_longlong()
+        check(L.goal_coarsener_smooth(h, float(target_quality), int(max_passes), ctypes.byref(nnz)))
+        X = np.zeros((N, 3))
+        org_n = np.zeros(N, np.int32)
+        T = np.zeros((E, 4), np.int32)
+        org_e = np.zeros(E, np.int32)
+        tri2 = np.zeros((len(tri), 3), np.int32)
+        tset2 = np.zeros(len(tri), np.int32)
+        check(L.goal_coarsener_get(h, _ptr(X), _ptr(org_n), _ptr(T), _ptr(org_e), _ptr(tri2), _ptr(tset2)))
+        ptr = np.zeros(N + 1, np.int32)
+        ids = np.zeros(nnz.value, np.int32)
+        w = np.zeros(nnz.value)
+        check(L.goal_coarsener_transfer(h, _ptr(ptr), _ptr(ids), _ptr(w)))
+    finally:
+        L.goal_coarsener_destroy(h)
+    out = Mesh(coords=X, tets=T, elem_set=np.asarray(mesh.elem_set).astype(np.int32),
+               elem_set_names=list(mesh.elem_set_names), node_sets=dict(mesh.node_sets),
+               side_sets={name: tri2[tset2 == i] for i, name in enumerate(names)})
+    return out, (ptr, ids, w)
+
+
+def apply_rows(values: np.ndarray, rows: Tuple[np.ndarray, ...]) -> np.ndarray:
+    """Nodal values through CSR transfer rows (ptr, ids, weights)."""
+    ptr, ids, w = rows
+    v = np.asarray(values, np.float64)
+    v = v.reshape(len(v), -1)
+    contrib = v[ids] * w[:, None]
+    out = np.add.reduceat(contrib, ptr[:-1], axis=0) if len(ids) else np.zeros((len(ptr) - 1, v.shape[1]))
+    return out
+
+
 class Transfer:
     """Moves nodal fields and element states from the mesh before an
     adaptation to the mesh after it: through the coarsening (kept nodes keep
@@ -178,15 +230,19 @@ class Transfer:
     means, children inherit)."""
 
     def __init__(self, node_origin: np.ndarray, elem_origin_c: np.ndarray, new_parents: np.ndarray,
-                 elem_origin_r: np.ndarray):
+                 elem_origin_r: np.ndarray, smooth_rows=None):
         self.node_origin = node_origin
         self.elem_origin_c = elem_origin_c
         self.new_parents = new_parents
         self.elem_origin_r = elem_origin_r
+        self.smooth_rows = smooth_rows
 
     def nodal(self, values: np.ndarray) -> np.ndarray:
         v = np.asarray(values, np.float64)
-        return transfer_nodal(v.reshape(len(v), -1)[self.node_origin], self.new_parents)
+        v = v.reshape(len(v), -1)[self.node_origin]
+        if self.smooth_rows is not None:
+            v = apply_rows(v, self.smooth_rows)
+        return transfer_nodal(v, self.new_parents)
 
     def states(self, states: Dict[str, np.ndarray]) -> Dict[str, np.ndarray]:
         return transfer_states(transfer_states(states, self.elem_origin_c), self.elem_origin_r)
@@ -201,18 +257,20 @@ def adapt_to_size(mesh: Mesh, vtx_size: np.ndarray, coarsen_ratio: float = 0.5, 
                   min_quality: float = 0.2, max_elems: int = 50_000_000,
                   improve_quality: float = 0.0) -> Tuple[Mesh, Transfer]:
     """One adaptation to a size field: coarsen (edges shorter than
-    coarsen_ratio x size), optionally flip around tets of quality below
-    improve_quality (0: no flips), then refine (edges longer than
-    refine_ratio x size). Returns the adapted mesh and the transfer of fields
-    onto it."""
+    coarsen_ratio x size), optionally improve the tets of quality below
+    improve_quality by flips and vertex smoothing (0: neither), then refine
+    (edges longer than refine_ratio x size). Returns the adapted mesh and the
+    transfer of fields onto it."""
     size = _f64(vtx_size)
     mc, org_n, org_ec = coarsen_to_size(mesh, size, ratio=coarsen_ratio, refine_ratio=refine_ratio,
                                         min_quality=min_quality)
+    rows = None
     if improve_quality > 0.0:
         mc, org_f = improve_shape(mc, target_quality=improve_quality)
         org_ec = np.asarray(org_ec)[org_f]
+        mc, rows = smooth(mc, target_quality=improve_quality)
     mr, parents, org_er = refine_to_size(mc, size[org_n], ratio=refine_ratio, max_elems=max_elems)
-    return mr, Transfer(org_n, org_ec, parents, org_er)
+    return mr, Transfer(org_n, org_ec, parents, org_er, rows)
 
 
 def _propagate(arr, base, new_parents, combine):

@@ -55,6 +55,9 @@ struct Coarsener {
   std::vector<int> S_set;
   std::vector<char> salive;
   std::vector<std::vector<int>> vs;
+  // nodal transfer of smoothing: a moved node's value is a combination of
+  // original nodes' values (empty: the node itself)
+  std::vector<std::vector<std::pair<int, double>>> W;
 
   double len2(int a, int b) const {
     const double dx = X[3 * a] - X[3 * b], dy = X[3 * a + 1] - X[3 * b + 1], dz = X[3 * a + 2] - X[3 * b + 2];
@@ -438,6 +441,118 @@ struct Coarsener {
     }
     return found ? best : 0.0;
   }
+  // ----- vertex smoothing (interior nodes of one element set) -----
+  double star_quality(int v) const {
+    double q = 1.0;
+    for (int t : vt[v])
+      if (talive[t]) q = std::min(q, quality(T[t]));
+    return q;
+  }
+  std::vector<std::pair<int, double>> row(int v) const {
+    if (W[v].empty()) return {{v, 1.0}};
+    return W[v];
+  }
+  // moves v to p if every tet of its star stays positive and the star's
+  // minimum quality rises; the value at v becomes the old field at p
+  bool try_move(int v, const double p[3]) {
+    const double keep[3] = {X[3 * v], X[3 * v + 1], X[3 * v + 2]};
+    const double q0 = star_quality(v);
+    // barycentric coordinates of p in the old star (before moving)
+    int host = -1;
+    double lam[4] = {0, 0, 0, 0};
+    double best = -1e300;
+    for (int t : vt[v]) {
+      if (!talive[t]) continue;
+      const auto& w = T[t];
+      const double V = vol6(w);
+      double l[4], lmin = 1e300;
+      for (int k = 0; k < 4; ++k) {
+        double e[3][3];
+        double P[4][3];
+        for (int q = 0; q < 4; ++q)
+          for (int c = 0; c < 3; ++c) P[q][c] = (q == k) ? p[c] : X[3 * w[q] + c];
+        for (int q = 0; q < 3; ++q)
+          for (int c = 0; c < 3; ++c) e[q][c] = P[q + 1][c] - P[0][c];
+        l[k] = (e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) - e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+                e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0])) / V;
+        lmin = std::min(lmin, l[k]);
+      }
+      if (lmin > best) {
+        best = lmin;
+        host = t;
+        for (int k = 0; k < 4; ++k) lam[k] = l[k];
+      }
+    }
+    if (host < 0 || best < -1e-12) return false;
+    for (int c = 0; c < 3; ++c) X[3 * v + c] = p[c];
+    bool ok = true;
+    double q1 = 1.0;
+    for (int t : vt[v]) {
+      if (!talive[t]) continue;
+      if (!(vol6(T[t]) > 0.0)) { ok = false; break; }
+      q1 = std::min(q1, quality(T[t]));
+    }
+    if (!ok || !(q1 > q0 * (1.0 + 1e-6))) {
+      for (int c = 0; c < 3; ++c) X[3 * v + c] = keep[c];
+      return false;
+    }
+    // compose the transfer rows (duplicates merged, order by node id)
+    std::vector<std::pair<int, double>> acc;
+    for (int k = 0; k < 4; ++k) {
+      if (lam[k] == 0.0) continue;
+      for (const auto& pr : row(T[host][k])) acc.push_back({pr.first, lam[k] * pr.second});
+    }
+    std::sort(acc.begin(), acc.end());
+    std::vector<std::pair<int, double>> merged;
+    for (const auto& pr : acc) {
+      if (!merged.empty() && merged.back().first == pr.first) merged.back().second += pr.second;
+      else merged.push_back(pr);
+    }
+    W[v] = merged;
+    return true;
+  }
+  int smooth_pass(double target_quality) {
+    std::vector<std::pair<double, int>> cand;
+    for (int v = 0; v < N; ++v) {
+      if (!valive[v] || cls[v] != 0) continue;  // interior, in no node or side set
+      int es = -1;
+      bool one = true;
+      for (int t : vt[v]) {
+        if (!talive[t]) continue;
+        if (es < 0) es = eset[t];
+        else if (eset[t] != es) one = false;
+      }
+      if (!one || es < 0) continue;
+      const double q = star_quality(v);
+      if (q < target_quality) cand.push_back({q, v});
+    }
+    std::sort(cand.begin(), cand.end());
+    std::vector<char> touched(N, 0);
+    std::vector<int> adj;
+    int done = 0;
+    for (const auto& qv : cand) {
+      const int v = qv.second;
+      if (touched[v]) continue;
+      adjacent(v, adj);
+      bool skip = false;
+      for (int x : adj) skip |= touched[x] != 0;
+      if (skip || adj.empty()) continue;
+      double p[3] = {0, 0, 0};
+      for (int x : adj)
+        for (int c = 0; c < 3; ++c) p[c] += X[3 * x + c] / (double)adj.size();
+      bool moved = try_move(v, p);
+      if (!moved) {
+        for (int c = 0; c < 3; ++c) p[c] = 0.5 * (p[c] + X[3 * v + c]);
+        moved = try_move(v, p);
+      }
+      if (!moved) continue;
+      touched[v] = 1;
+      for (int x : adj) touched[x] = 1;
+      ++done;
+    }
+    return done;
+  }
+
   int swap_pass(double target_quality) {
     std::vector<std::pair<double, int>> bad;
     for (size_t t = 0; t < T.size(); ++t)
@@ -540,6 +655,7 @@ int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, co
     c.vt.assign(num_nodes, {});
     c.vf.assign(num_nodes, {});
     c.vs.assign(num_nodes, {});
+    c.W.assign(num_nodes, {});
     // boundary faces: the faces of exactly one tet (sorted vertex triples,
     // sorted, counted by runs)
     static const int kFaces[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
@@ -647,6 +763,53 @@ int goal_coarsener_swap(goal_coarsener h, double target_quality, int max_passes,
     sizes[0] = nn;
     sizes[1] = ne;
     sizes[2] = ns;
+  } catch (const goal::Error& e) {
+    goal::set_last_error(e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    goal::set_last_error(e.what());
+    return GOAL_ERR_STATE;
+  }
+  return GOAL_OK;
+}
+
+int goal_coarsener_smooth(goal_coarsener h, double target_quality, int max_passes, long long* transfer_nnz) {
+  try {
+    if (!h || !transfer_nnz || !(target_quality > 0.0) || target_quality > 1.0)
+      throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_smooth: bad arguments");
+    goal::Coarsener& c = h->c;
+    for (int p = 0; p < max_passes; ++p)
+      if (c.smooth_pass(target_quality) == 0) break;
+    long long nnz = 0;
+    for (int n = 0; n < c.N; ++n)
+      if (c.valive[n]) nnz += c.W[n].empty() ? 1 : (long long)c.W[n].size();
+    *transfer_nnz = nnz;
+  } catch (const goal::Error& e) {
+    goal::set_last_error(e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    goal::set_last_error(e.what());
+    return GOAL_ERR_STATE;
+  }
+  return GOAL_OK;
+}
+
+int goal_coarsener_transfer(goal_coarsener h, int* ptr, int* ids, double* weights) {
+  try {
+    if (!h || !ptr || !ids || !weights) throw goal::Error(GOAL_ERR_ARG, "goal_coarsener_transfer: bad arguments");
+    const goal::Coarsener& c = h->c;
+    long long k = 0;
+    int row = 0;
+    ptr[0] = 0;
+    for (int n = 0; n < c.N; ++n) {
+      if (!c.valive[n]) continue;
+      for (const auto& pr : c.row(n)) {
+        ids[k] = pr.first;
+        weights[k] = pr.second;
+        ++k;
+      }
+      ptr[++row] = (int)k;
+    }
   } catch (const goal::Error& e) {
     goal::set_last_error(e.what());
     return e.code;

@@ -164,6 +164,16 @@ int goal_coarsener_coarsen(goal_coarsener c, const double* vtx_size, double rati
  * triangles. A new tet takes the original element of the old tet that holds
  * its centroid. sizes as for coarsen. Callable with or without coarsen. */
 int goal_coarsener_swap(goal_coarsener c, double target_quality, int max_passes, long long* sizes);
+/* Vertex smoothing: interior nodes (in no node or side set, inside one
+ * element set) whose surrounding tets have a quality below target_quality,
+ * worst first and one independent set per pass, move to the mean of their
+ * neighbours (or halfway there) when every tet around stays positive and the
+ * worst quality around rises. A moved node's value becomes the old field at
+ * its new position: transfer gives, per kept node (in the order of get), the
+ * original nodes and weights (CSR: ptr[nodes + 1], ids/weights[nnz], nnz from
+ * transfer_nnz); linear fields move exactly. */
+int goal_coarsener_smooth(goal_coarsener c, double target_quality, int max_passes, long long* transfer_nnz);
+int goal_coarsener_transfer(goal_coarsener c, int* ptr, int* ids, double* weights);
 int goal_coarsener_get(goal_coarsener c, double* coords, int* node_origin, int* tets, int* elem_origin, int* tris,
                        int* tri_set);
 int goal_coarsener_destroy(goal_coarsener c);

@@ -1,5 +1,5 @@
 """Coarsening by edge collapse (the coarsening half of goal's adaptation
-step), shape improvement by 2-3 / 3-2 flips, and the coarsen-then-refine
+step), shape improvement by 2-3 / 3-2 flips and vertex smoothing, and the coarsen-then-refine
 adaptation with its field transfer. Host code, run on the CPU: conformity,
 positive orientation, volume (per element set) and boundary area preserved,
 boundary nodes and side sets kept on their planes, the length and quality
@@ -167,3 +167,41 @@ def test_flips_after_coarsening_keep_the_mesh_valid():
         assert abs(_area(out.coords, out.side_sets[name]) - 1.0) < 1e-12
         assert all(tuple(sorted(t)) in bnd for t in out.side_sets[name])
     assert origin.min() >= 0 and origin.max() < mc.num_elems
+
+
+def test_smoothing_raises_quality_and_moves_linear_fields_exactly():
+    mesh = kuhn_cube(10, jitter=0.25, seed=3)
+    out, rows = adapt.smooth(mesh, target_quality=0.35)
+    assert np.array_equal(out.tets, mesh.tets)
+    _check_conforming(out)
+    v = _volumes(out)
+    assert v.min() > 0 and abs(v.sum() - 1.0) < 1e-12
+    q0, q1 = _quality(mesh), _quality(out)
+    assert q1.min() > q0.min() + 0.05
+    moved = np.any(out.coords != mesh.coords, axis=1)
+    assert moved.sum() > 0
+    # boundary and set nodes stay put
+    for name, nodes in mesh.node_sets.items():
+        assert not moved[nodes].any()
+    # a linear field moves exactly; unmoved nodes keep their values
+    g = np.array([1.0, -2.0, 0.5])
+    lin = np.stack([mesh.coords @ g + 3.0, mesh.coords[:, 2]], axis=1)
+    t = adapt.apply_rows(lin, rows)
+    assert np.allclose(t[:, 0], out.coords @ g + 3.0, atol=1e-12)
+    assert np.allclose(t[:, 1], out.coords[:, 2], atol=1e-12)
+    assert np.array_equal(t[~moved], lin[~moved])
+
+
+def test_adapt_with_shape_improvement():
+    mesh = kuhn_cube(8, jitter=0.2, seed=1)
+    r = np.linalg.norm(mesh.coords, axis=1)
+    size = 0.05 + 0.4 * r
+    out, tr = adapt.adapt_to_size(mesh, size, improve_quality=0.35)
+    _check_conforming(out)
+    v = _volumes(out)
+    assert v.min() > 0 and abs(v.sum() - 1.0) < 1e-12
+    g = np.array([0.3, 1.0, -0.7])
+    t = tr.nodal(mesh.coords @ g)
+    assert np.allclose(t[:, 0], out.coords @ g, atol=1e-12)
+    st = tr.states({"eqps": np.arange(mesh.num_elems, dtype=float)})
+    assert st["eqps"].shape == (out.num_elems,)
