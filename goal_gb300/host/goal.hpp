@@ -357,13 +357,17 @@ inline CoarsenedMesh coarsen_to_size(const std::vector<double>& coords, const st
                                      const std::vector<int>& elem_set, const std::vector<long long>& node_class,
                                      const std::vector<int>& tris, const std::vector<int>& tri_set,
                                      const std::vector<double>& vtx_size, double ratio = 0.5,
-                                     double refine_ratio = 1.5, double min_quality = 0.2, int max_passes = 8) {
+                                     double refine_ratio = 1.5, double min_quality = 0.2, int max_passes = 8,
+                                     double improve_quality = 0.0) {
   goal_coarsener c = nullptr;
   check(goal_coarsener_create((int)(coords.size() / 3), coords.data(), (int)(tets.size() / 4), tets.data(),
                               elem_set.empty() ? nullptr : elem_set.data(), node_class.data(), (int)tri_set.size(),
                               tris.data(), tri_set.data(), &c));
   long long sizes[3];
   int rc = goal_coarsener_coarsen(c, vtx_size.data(), ratio, refine_ratio, min_quality, max_passes, sizes);
+  // optional shape improvement: flips (vertex smoothing would move nodes and
+  // needs the interpolating transfer of goal_coarsener_transfer)
+  if (rc == GOAL_OK && improve_quality > 0.0) rc = goal_coarsener_swap(c, improve_quality, 4, sizes);
   if (rc != GOAL_OK) {
     goal_coarsener_destroy(c);
     check(rc);

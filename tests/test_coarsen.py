@@ -205,3 +205,27 @@ def test_adapt_with_shape_improvement():
     assert np.allclose(t[:, 0], out.coords @ g, atol=1e-12)
     st = tr.states({"eqps": np.arange(mesh.num_elems, dtype=float)})
     assert st["eqps"].shape == (out.num_elems,)
+
+
+def test_bad_arguments_are_errors():
+    import ctypes
+    from goal_gb300 import lib
+    from goal_gb300.api import GoalError, check
+    L = lib()
+    h = ctypes.c_void_p()
+    X = np.zeros(12)
+    T = np.array([0, 1, 2, 4], np.int32)  # node 4 of 4
+    cls = np.zeros(4, np.int64)
+    rc = L.goal_coarsener_create(4, X.ctypes.data, 1, T.ctypes.data, None, cls.ctypes.data, 0, None, None,
+                                 ctypes.byref(h))
+    assert rc != 0
+    try:
+        check(rc)
+        raise AssertionError("expected an error")
+    except GoalError as e:
+        assert "out of range" in str(e)
+    mesh = kuhn_cube(2)
+    with np.testing.assert_raises(Exception):
+        adapt.coarsen_to_size(mesh, np.zeros(mesh.num_nodes))  # sizes must be positive
+    with np.testing.assert_raises(ValueError):
+        adapt.coarsen_to_size(mesh, np.ones(3))
