@@ -125,13 +125,19 @@ class Disc:
 class Mechanics:
     """Model, materials, integration-point states and the nodal solution."""
 
-    def __init__(self, disc: Disc, model: int, materials: Sequence[Sequence[float]], stabilization: bool = True):
+    def __init__(self, disc: Disc, model: int, materials: Sequence[Sequence[float]], stabilization: bool = True,
+                 fp_reset: bool = False):
+        """``fp_reset``: J2 writes Fp = Fp_old at points that end elastic (goal
+        keeps an earlier plastic Newton iterate's Fp there; see
+        goal_mechanics_set_fp_reset)."""
         self.disc = disc
         self.model = model
         mats = _f64(materials).reshape(-1, 5)
         h = ctypes.c_void_p()
         check(lib().goal_mechanics_create(disc.h, model, _ptr(mats), int(stabilization), ctypes.byref(h)))
         self.h = h
+        if fp_reset:
+            check(lib().goal_mechanics_set_fp_reset(self.h, 1))
 
     def set_solution(self, U: np.ndarray):
         U = _f64(U).reshape(-1)
@@ -278,7 +284,7 @@ def eval_expr(expr: str, x: float, y: float, z: float, t: float) -> float:
     return out.value
 
 
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_F32, NESTED_F64 = 0, 1, 2, 3  # precision: FP64; inner solve in binary16 / FP32 / FP64
 PRECOND_BJ, PRECOND_LEARNED = 0, 1
 
 

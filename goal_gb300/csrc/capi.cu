@@ -152,8 +152,8 @@ static SolveParams to_params(const goal_solve_params* p) {
   GOAL_REQUIRE(q.krylov_size >= 1 && q.krylov_size < 256, GOAL_ERR_ARG, "krylov size must be in [1, 255]");
   GOAL_REQUIRE(q.max_iters >= 1, GOAL_ERR_ARG, "max iters must be >= 1");
   GOAL_REQUIRE(q.tolerance > 0.0, GOAL_ERR_ARG, "tolerance must be > 0");
-  GOAL_REQUIRE(q.precision == PREC_FP64 || q.precision == PREC_MIXED, GOAL_ERR_ARG, "unknown precision mode");
-  GOAL_REQUIRE(q.precision == PREC_FP64 || (q.inner_iters >= 1 && q.inner_iters < 256), GOAL_ERR_ARG,
+  GOAL_REQUIRE(q.precision >= PREC_FP64 && q.precision <= PREC_NESTED_F64, GOAL_ERR_ARG, "unknown precision mode");
+  GOAL_REQUIRE(!has_inner_solve(q.precision) || (q.inner_iters >= 1 && q.inner_iters < 256), GOAL_ERR_ARG,
                "inner iterations must be in [1, 255]");
   return q;
 }
@@ -321,6 +321,20 @@ int goal_disc_stream(goal_disc d, void** stream) {
   GOAL_API_END
 }
 
+int goal_disc_device_graph(goal_disc d, const int** brow_ptr, const int** bcol, const int** row_ptr,
+                           const int** col_idx) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && d->d->built, "goal_disc_device_graph: disc not built");
+  if (brow_ptr) *brow_ptr = d->d->brow_ptr.ptr;
+  if (bcol) *bcol = d->d->bcol.ptr;
+  if (row_ptr || col_idx) {
+    d->d->csr_graph_device();
+    if (row_ptr) *row_ptr = d->d->csr_row_ptr.ptr;
+    if (col_idx) *col_idx = d->d->csr_col_idx.ptr;
+  }
+  GOAL_API_END
+}
+
 int goal_disc_destroy(goal_disc d) {
   GOAL_API_BEGIN
   delete d;
@@ -395,6 +409,20 @@ int goal_mechanics_get_solution(goal_mechanics m, double* U) {
   GOAL_ARG(m && U, "null argument");
   m->m->U.download(U, m->m->disc->stream);
   GOAL_CUDA(cudaStreamSynchronize(m->m->disc->stream));
+  GOAL_API_END
+}
+
+int goal_mechanics_set_fp_reset(goal_mechanics m, int on) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m, "goal_mechanics_set_fp_reset: null handle");
+  m->m->fp_reset = on != 0;
+  GOAL_API_END
+}
+
+int goal_mechanics_device_solution(goal_mechanics m, double** U) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && U, "goal_mechanics_device_solution: null argument");
+  *U = m->m->U.ptr;
   GOAL_API_END
 }
 
@@ -490,6 +518,30 @@ int goal_sol_info_get_dRdu_bsr(goal_sol_info s, double* values) {
   cudaStream_t st = s->s->disc->stream;
   s->s->A.download(values, st);
   GOAL_CUDA(cudaStreamSynchronize(st));
+  GOAL_API_END
+}
+
+int goal_sol_info_device_view(goal_sol_info s, double** R, double** dMdu, double** bsr_vals) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s, "goal_sol_info_device_view: null handle");
+  if (R) *R = s->s->R.ptr;
+  if (dMdu) *dMdu = s->s->dMdu.ptr;
+  if (bsr_vals) *bsr_vals = s->s->A.ptr;
+  GOAL_API_END
+}
+
+int goal_sol_info_device_csr(goal_sol_info s, double** csr_vals) {
+  GOAL_API_BEGIN
+  GOAL_ARG(s && csr_vals, "goal_sol_info_device_csr: null argument");
+  const Disc& d = *s->s->disc;
+  GOAL_REQUIRE(d.nnz <= 2147483647ll, GOAL_ERR_CAPACITY,
+               "goal_sol_info_device_csr: more than 2^31-1 nonzeros for int32 indices");
+  s->s->csr.alloc(d.nnz);
+  k_bsr_to_csr<<<grid_for(d.num_nodes, 128), 128, 0, d.stream>>>(d.num_nodes, d.brow_ptr.ptr, s->s->A.ptr,
+                                                                 s->s->csr.ptr);
+  GOAL_CHECK_LAUNCH();
+  GOAL_CUDA(cudaStreamSynchronize(d.stream));
+  *csr_vals = s->s->csr.ptr;
   GOAL_API_END
 }
 

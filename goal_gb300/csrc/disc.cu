@@ -499,6 +499,17 @@ void Disc::csr_graph(int* row_ptr_h, int* col_idx_h) const {
   GOAL_CUDA(cudaStreamSynchronize(stream));
 }
 
+void Disc::csr_graph_device() {
+  if (csr_row_ptr.ptr) return;
+  GOAL_REQUIRE(nnz <= 2147483647ll, GOAL_ERR_CAPACITY, "scalar CSR graph: more than 2^31-1 nonzeros for int32 indices");
+  csr_row_ptr.alloc(4ll * num_nodes + 1);
+  csr_col_idx.alloc(nnz);
+  k_csr_expand<<<grid_for(num_nodes, 128), 128, 0, stream>>>(num_nodes, brow_ptr.ptr, bcol.ptr, csr_row_ptr.ptr,
+                                                             csr_col_idx.ptr);
+  GOAL_CHECK_LAUNCH();
+  GOAL_CUDA(cudaStreamSynchronize(stream));
+}
+
 // ------------------------------------------------------------------ nested
 namespace {
 

@@ -99,9 +99,14 @@ struct Disc {
   DevBuf<int> parent_edges;    // (num_nodes - base_nodes) x 2: edge end points of new nodes
   int base_elems = 0;          // children of base element e are 8e..8e+7 (original order)
 
+  // the scalar CSR graph kept on the device (4N+1 row pointers, nnz columns),
+  // built on the first request for device pointers
+  DevBuf<int> csr_row_ptr, csr_col_idx;
+
   void build();                // Disc::build_data: graph, colouring, geometry
   DiscView view() const;
   void csr_graph(int* row_ptr, int* col_idx) const;  // host outputs
+  void csr_graph_device();     // fills csr_row_ptr / csr_col_idx once
 };
 
 // Builds the uniformly refined nested mesh of ``base`` on the device

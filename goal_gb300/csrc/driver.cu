@@ -141,7 +141,7 @@ BsrView bsr_view(const Disc& d) {
 SolveStats linear_solve(SolInfo& s, const SolveParams& p, const double* b, double* x, Krylov& K, const double* dD) {
   K.stream = s.disc->stream;
   BsrView A = bsr_view(*s.disc);
-  if (p.precision == PREC_MIXED) make_inner_copy(A, s.A.ptr, K);
+  if (has_inner_solve(p.precision)) make_inner_copy(A, s.A.ptr, p.precision, K);
   if (p.precond == PRECOND_LEARNED) {
     GOAL_REQUIRE(s.learned, GOAL_ERR_STATE, "learned preconditioner requested but no network is attached");
     s.learned->stream = K.stream;
@@ -228,6 +228,7 @@ void NestedAdjoint::build(Mechanics& base_mech) {
   mech->disc = disc.get();
   mech->model = base_mech.model;
   mech->stabilization = base_mech.stabilization;
+  mech->fp_reset = base_mech.fp_reset;
   mech->mats_h = base_mech.mats_h;
   mech->init();
   si = std::make_unique<SolInfo>();

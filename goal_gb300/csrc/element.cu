@@ -66,6 +66,7 @@ struct ElemArgs {
   int estride;
   int begin, end;
   int stab, save, overwrite, qoi;
+  int fp_reset;    // also write Fp = Fp_old at elastic points (goal leaves Fp as it was)
   double rho, ks_max, ks_scale;
 };
 
@@ -264,6 +265,10 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       }
     } else if (a.save) {
       a.eqps[s] = eq_old;
+      if (a.fp_reset) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) a.Fp[q * E + s] = __ldg(a.Fp_old + q * E + s);
+      }
     }
   }
 
@@ -860,6 +865,7 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
   a.status = m.status.ptr;
   a.stab = m.stabilization ? 1 : 0;
   a.save = c.save_states;
+  a.fp_reset = m.fp_reset ? 1 : 0;
   a.overwrite = c.overwrite;
   a.qoi = c.qoi;
   a.rho = c.rho;

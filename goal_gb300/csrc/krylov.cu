@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256) k_spmv_col(int N, const int* __restrict__
 // by shuffles. z goes to out, not over x: other quads still read z1. Same
 // arithmetic as k_spmv_col followed by k_second_sweep_col.
 template <typename T, typename TA, typename TV>
-__global__ void __launch_bounds__(256, 8) k_spmv_sweep(int N, const int* __restrict__ brow_ptr,
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 4 : 8) k_spmv_sweep(int N, const int* __restrict__ brow_ptr,
                                                     const int* __restrict__ bcol, const TA* __restrict__ A,
                                                     const T* __restrict__ x, const T* __restrict__ B, const TV* V,
                                                     long long ldv, const GState* st, T* __restrict__ out) {
@@ -810,15 +810,17 @@ __global__ void k_scale_into(long long n, const TR* r, const GState* st, T* v0) 
 }
 
 // The inner solve works in the dof-scaled space: r^ = S r in, z = S z^ out.
-__global__ void k_col_to_f32(long long n, const double* V, long long ld, const GState* st, const double* sd,
-                             float* out) {
+template <typename T>
+__global__ void k_col_to_inner(long long n, const double* V, long long ld, const GState* st, const double* sd,
+                               T* out) {
   if (st->done) return;
   const double* v = V + (long long)st->j * ld;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    out[i] = (float)(v[i] * sd[i]);
+    out[i] = (T)(v[i] * sd[i]);
 }
-__global__ void k_f32_to_col(long long n, const float* in, const double* sd, double* Z, long long ld,
-                             const GState* st) {
+template <typename T>
+__global__ void k_inner_to_col(long long n, const T* in, const double* sd, double* Z, long long ld,
+                               const GState* st) {
   if (st->done) return;
   double* z = Z + (long long)st->j * ld;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -896,31 +898,38 @@ __global__ void k_dof_scale(int N, const int* __restrict__ diag, const double* _
     sd[i] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
   }
 }
-// A^ = S A S in binary16 (saturated to the finite range); thread = (node, row)
-__global__ void k_to_half_scaled(int N, const int* __restrict__ brow_ptr, const int* __restrict__ bcol,
-                                 const double* __restrict__ A, const double* __restrict__ sd, __half* A16) {
+// A^ = S A S in the inner storage type (binary16 saturated to its finite
+// range); thread = (node, row)
+template <typename TA>
+__device__ __forceinline__ TA to_storage(double v) {
+  return (TA)v;
+}
+template <>
+__device__ __forceinline__ __half to_storage<__half>(double v) {
+  return __double2half(fmin(fmax(v, -65504.0), 65504.0));
+}
+template <typename TA>
+__global__ void k_to_scaled(int N, const int* __restrict__ brow_ptr, const int* __restrict__ bcol,
+                            const double* __restrict__ A, const double* __restrict__ sd, TA* As) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 4 * N; t += gridDim.x * blockDim.x) {
     const int n = t >> 2, r = t & 3;
     const double sr = sd[t];
     for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
       const int m = bcol[k];
-      for (int c = 0; c < 4; ++c) {
-        double v = sr * A[16ll * k + 4 * r + c] * sd[4ll * m + c];
-        v = fmin(fmax(v, -65504.0), 65504.0);
-        A16[16ll * k + 4 * r + c] = __double2half(v);
-      }
+      for (int c = 0; c < 4; ++c) As[16ll * k + 4 * r + c] = to_storage<TA>(sr * A[16ll * k + 4 * r + c] * sd[4ll * m + c]);
     }
   }
 }
 // the preconditioner blocks in the scaled space: D^-1 -> S^-1 D^-1 S^-1 and
-// (learned second sweep) B -> S^-1 B S^-1, in FP32
+// (learned second sweep) B -> S^-1 B S^-1, in the inner arithmetic type
+template <typename T>
 __global__ void k_inner_blocks(int N, const double* __restrict__ Dinv, const double* __restrict__ Bc,
-                               const double* __restrict__ sd, float* Dinv32, float* Bc32) {
+                               const double* __restrict__ sd, T* Dinv_s, T* Bc_s) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) {
     const int n = i >> 4, r = (i >> 2) & 3, c = i & 3;
     const double s = sd[4ll * n + r] * sd[4ll * n + c];
-    Dinv32[i] = (float)(Dinv[i] / s);
-    if (Bc) Bc32[i] = (float)(Bc[i] / s);
+    Dinv_s[i] = (T)(Dinv[i] / s);
+    if (Bc) Bc_s[i] = (T)(Bc[i] / s);
   }
 }
 
@@ -954,7 +963,8 @@ Krylov::~Krylov() {
   if (h_scal) cudaFreeHost(h_scal);
 }
 
-void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
+void Krylov::reserve(int n_, int m_, int mi_, int precision, int nnzb) {
+  (void)nnzb;
   GOAL_REQUIRE(m_ >= 1 && m_ < kMaxM && mi_ >= 1 && mi_ < kMaxM, GOAL_ERR_ARG, "krylov size must be in [1, 255]");
   if (!h_scal) GOAL_CUDA(cudaMallocHost(&h_scal, 64 * sizeof(double)));
   const size_t nn = (size_t)n_;
@@ -971,17 +981,25 @@ void Krylov::reserve(int n_, int m_, int mi_, bool mixed, int nnzb) {
   need(scal, 64);
   need(flag, 8);
   need(dots, kMaxM + 2);
-  if (mixed) {
-    need(V16, nn * (mi_ + 1));
-    need(w32, nn);
-    need(r32, nn);
-    need(t32, nn);
+  if (has_inner_solve(precision)) {
+    const size_t nb = nn * (mi_ + 1);
+    if (precision == PREC_MIXED) need(V16, nb);
+    if (precision == PREC_MIXED_F32) need(V32, nb);
+    if (precision == PREC_NESTED_F64) {
+      need(V64, nb);
+      need(w64, nn);
+      need(r64, nn);
+      need(t64, nn);
+    } else {
+      need(w32, nn);
+      need(r32, nn);
+      need(t32, nn);
+    }
     need(Hi, (size_t)(mi_ + 1) * mi_);
     need(csi, mi_ + 1);
     need(sni, mi_ + 1);
     need(gi, mi_ + 2);
     need(yi, mi_ + 1);
-
   }
   n = n_;
   m = m_;
@@ -1002,13 +1020,28 @@ int block_jacobi_setup(const BsrView& A, const double* vals, const double* dD, K
   return sing;
 }
 
-void make_inner_copy(const BsrView& A, const double* vals, Krylov& K) {
+void make_inner_copy(const BsrView& A, const double* vals, int precision, Krylov& K) {
   const int N = A.num_nodes;
   need(K.sd, 4ull * N);
-  need(K.A16, 16ull * A.nnzb);
   k_dof_scale<<<grid_for(4ll * N, 256), 256, 0, K.stream>>>(N, A.diag, vals, K.sd.ptr);
   GOAL_CHECK_LAUNCH();
-  k_to_half_scaled<<<grid_for(4ll * N, 256), 256, 0, K.stream>>>(N, A.brow_ptr, A.bcol, vals, K.sd.ptr, K.A16.ptr);
+  const int g = grid_for(4ll * N, 256);
+  switch (precision) {
+    case PREC_MIXED:
+      need(K.A16, 16ull * A.nnzb);
+      k_to_scaled<__half><<<g, 256, 0, K.stream>>>(N, A.brow_ptr, A.bcol, vals, K.sd.ptr, K.A16.ptr);
+      break;
+    case PREC_MIXED_F32:
+      need(K.A32, 16ull * A.nnzb);
+      k_to_scaled<float><<<g, 256, 0, K.stream>>>(N, A.brow_ptr, A.bcol, vals, K.sd.ptr, K.A32.ptr);
+      break;
+    case PREC_NESTED_F64:
+      need(K.A64, 16ull * A.nnzb);
+      k_to_scaled<double><<<g, 256, 0, K.stream>>>(N, A.brow_ptr, A.bcol, vals, K.sd.ptr, K.A64.ptr);
+      break;
+    default:
+      throw Error(GOAL_ERR_ARG, "make_inner_copy: no inner solve in this precision mode");
+  }
   GOAL_CHECK_LAUNCH();
 }
 
@@ -1123,38 +1156,136 @@ struct StepGraph {
 };
 }  // namespace
 
+namespace {
+
+// The inner solve's arrays for one storage / arithmetic combination: matrix
+// (TA), basis (TV), work vectors, block-Jacobi blocks and the small Hessenberg
+// state in the arithmetic type T (FP32 state lives in the FP64 buffers
+// reserved for it).
+template <typename T, typename TA, typename TV>
+struct Inner {
+  const TA* A;
+  TV* V;
+  T *r, *w, *t;
+  const T *Dinv, *Bc;
+  T *H, *cs, *sn, *g, *y, *dots, *red;
+};
+
+template <typename T>
+T* as_t(double* p) {
+  return reinterpret_cast<T*>(p);
+}
+
+Inner<float, __half, __half> inner_arrays(Krylov& K, __half*) {
+  return {K.A16.ptr, K.V16.ptr, K.r32.ptr, K.w32.ptr, K.t32.ptr, K.Dinv32.ptr, K.Bc32.ptr, as_t<float>(K.Hi.ptr),
+          as_t<float>(K.csi.ptr), as_t<float>(K.sni.ptr), as_t<float>(K.gi.ptr), as_t<float>(K.yi.ptr),
+          as_t<float>(K.dots.ptr), as_t<float>(K.red.ptr)};
+}
+Inner<float, float, float> inner_arrays(Krylov& K, float*) {
+  return {K.A32.ptr, K.V32.ptr, K.r32.ptr, K.w32.ptr, K.t32.ptr, K.Dinv32.ptr, K.Bc32.ptr, as_t<float>(K.Hi.ptr),
+          as_t<float>(K.csi.ptr), as_t<float>(K.sni.ptr), as_t<float>(K.gi.ptr), as_t<float>(K.yi.ptr),
+          as_t<float>(K.dots.ptr), as_t<float>(K.red.ptr)};
+}
+Inner<double, double, double> inner_arrays(Krylov& K, double*) {
+  return {K.A64.ptr, K.V64.ptr, K.r64.ptr, K.w64.ptr, K.t64.ptr, K.Dinv64s.ptr, K.Bc64s.ptr, K.Hi.ptr, K.csi.ptr,
+          K.sni.ptr, K.gi.ptr, K.yi.ptr, K.dots.ptr, K.red.ptr};
+}
+
+// The scaled block-Jacobi (and second-sweep) blocks of the inner solve.
+void inner_blocks(int N, int precision, Krylov& K) {
+  const bool two = K.two_sweep;
+  if (precision == PREC_NESTED_F64) {
+    need(K.Dinv64s, 16ull * N);
+    if (two) need(K.Bc64s, 16ull * N);
+    k_inner_blocks<double><<<grid_for(16ll * N, 256), 256, 0, K.stream>>>(N, K.Dinv.ptr, two ? K.Bc.ptr : nullptr,
+                                                                          K.sd.ptr, K.Dinv64s.ptr, K.Bc64s.ptr);
+  } else {
+    need(K.Dinv32, 16ull * N);
+    if (two) need(K.Bc32, 16ull * N);
+    k_inner_blocks<float><<<grid_for(16ll * N, 256), 256, 0, K.stream>>>(N, K.Dinv.ptr, two ? K.Bc.ptr : nullptr,
+                                                                         K.sd.ptr, K.Dinv32.ptr, K.Bc32.ptr);
+  }
+  GOAL_CHECK_LAUNCH();
+}
+
+// The outer step's preconditioner application Z_j = M^-1 V_j: mi inner GMRES
+// iterations in the dof-scaled space with the right block-Jacobi (or learned
+// two-sweep) preconditioner, Z_j = S M^-1 V_in y with V_in the inner basis
+// started from S V_j. Every kernel is gated on the outer state st.
+template <typename T, typename TA, typename TV>
+void issue_inner(const BsrView& A, long long n, int mi, bool sweep2, GState* st, GState* sti, Krylov& K,
+                 const Inner<T, TA, TV>& in) {
+  const int N = A.num_nodes;
+  const int nbx = vec_grid(n);
+  cudaStream_t s = K.stream;
+  k_col_to_inner<T><<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.sd.ptr, in.r);
+  GOAL_CHECK_LAUNCH();
+  k_norm2_part<T><<<nbx, 256, 0, s>>>(n, in.r, in.red);
+  GOAL_CHECK_LAUNCH();
+  k_cycle_fin<T><<<1, 256, 0, s>>>(nbx, in.red, sti, in.g, mi, nullptr);
+  GOAL_CHECK_LAUNCH();
+  k_gate<<<1, 1, 0, s>>>(st, sti);
+  GOAL_CHECK_LAUNCH();
+  k_scale_into<TV, T><<<nbx, 256, 0, s>>>(n, in.r, sti, in.V);
+  GOAL_CHECK_LAUNCH();
+  // r = D^-1 v_0; later steps get D^-1 v_it from the normalization
+  k_bj_colin<T, TV><<<grid_for(n, 256), 256, 0, s>>>(N, in.Dinv, in.V, n, sti, in.r);
+  GOAL_CHECK_LAUNCH();
+  for (int it = 0; it < mi; ++it) {
+    // z = M^-1 v_it (in t with the second sweep, else r); w = A^ z
+    T* z = in.r;
+    if (sweep2) {
+      k_spmv_sweep<T, TA, TV><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, in.A, in.r, in.Bc, in.V, n, sti,
+                                                           in.t);
+      GOAL_CHECK_LAUNCH();
+      z = in.t;
+    }
+    k_spmv_col<T, TA><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, in.A, z, 0, sti, in.w);
+    GOAL_CHECK_LAUNCH();
+    // orthogonalize, normalize into v_{it+1}, and r = D^-1 v_{it+1}
+    arnoldi_orth<T, TV>(n, in.V, in.w, sti, in.H, mi + 1, in.cs, in.sn, in.g, in.dots, in.red, mi, 0.0, kInnerPasses,
+                        s, in.Dinv, in.r);
+  }
+  k_backsolve<T><<<1, 32, 0, s>>>(sti, in.H, mi + 1, in.g, in.y);
+  GOAL_CHECK_LAUNCH();
+  k_combine<TV, T><<<nbx, 256, 0, s>>>(n, in.V, n, in.y, sti, in.w, 1);
+  GOAL_CHECK_LAUNCH();
+  k_bj<T><<<grid_for(n, 256), 256, 0, s>>>(N, in.Dinv, in.w, in.r);
+  GOAL_CHECK_LAUNCH();
+  if (sweep2) {
+    k_spmv<T, TA, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, in.A, in.r, nullptr, in.t);
+    GOAL_CHECK_LAUNCH();
+    k_second_sweep_col<T, T><<<grid_for(n, 256), 256, 0, s>>>(N, in.Bc, in.w, 0, in.t, in.r, 0, nullptr);
+    GOAL_CHECK_LAUNCH();
+  }
+  k_inner_to_col<T><<<nbx, 256, 0, s>>>(n, in.r, K.sd.ptr, K.Z.ptr, n, st);
+  GOAL_CHECK_LAUNCH();
+}
+
+}  // namespace
+
 SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double* x, const SolveParams& p, Krylov& K) {
   auto t0 = std::chrono::steady_clock::now();
   SolveStats out;
   const int N = A.num_nodes;
   const long long n = 4ll * N;
-  const bool mixed = p.precision == PREC_MIXED;
+  const bool mixed = has_inner_solve(p.precision);
   const int m = p.krylov_size;
   const int mi = std::max(1, p.inner_iters);
-  K.reserve((int)n, m, mi, mixed, A.nnzb);
+  K.reserve((int)n, m, mi, p.precision, A.nnzb);
   cudaStream_t s = K.stream;
   GOAL_REQUIRE(K.Dinv.ptr, GOAL_ERR_STATE, "fgmres: block-Jacobi preconditioner not set up");
   if (mixed) {
-    GOAL_REQUIRE(K.A16.ptr && K.sd.ptr, GOAL_ERR_STATE, "fgmres: inner matrix copy missing");
-    need(K.Dinv32, 16ull * N);
-    if (K.two_sweep) need(K.Bc32, 16ull * N);
-    k_inner_blocks<<<grid_for(16ll * N, 256), 256, 0, s>>>(N, K.Dinv.ptr, K.two_sweep ? K.Bc.ptr : nullptr, K.sd.ptr,
-                                                          K.Dinv32.ptr, K.Bc32.ptr);
-    GOAL_CHECK_LAUNCH();
+    const bool have = K.sd.ptr && ((p.precision == PREC_MIXED && K.A16.ptr) ||
+                                   (p.precision == PREC_MIXED_F32 && K.A32.ptr) ||
+                                   (p.precision == PREC_NESTED_F64 && K.A64.ptr));
+    GOAL_REQUIRE(have, GOAL_ERR_STATE, "fgmres: inner matrix copy missing");
+    inner_blocks(N, p.precision, K);
   }
 
   GState* st = reinterpret_cast<GState*>(K.scal.ptr);         // outer state
   GState* sti = reinterpret_cast<GState*>(K.scal.ptr + 24);   // inner state
   double* dots = K.dots.ptr;
-  // the inner solve's Hessenberg matrix, rotations, partial sums and dot
-  // products are FP32 (in the FP64 buffers reserved for them)
-  float* Hin = mixed ? reinterpret_cast<float*>(K.Hi.ptr) : nullptr;
-  float* csin = mixed ? reinterpret_cast<float*>(K.csi.ptr) : nullptr;
-  float* snin = mixed ? reinterpret_cast<float*>(K.sni.ptr) : nullptr;
-  float* gin = mixed ? reinterpret_cast<float*>(K.gi.ptr) : nullptr;
-  float* yin = mixed ? reinterpret_cast<float*>(K.yi.ptr) : nullptr;
-  float* dots32 = reinterpret_cast<float*>(K.dots.ptr);
-  float* red32 = reinterpret_cast<float*>(K.red.ptr);
 
   const double bnorm = read_norm(n, b, K);
   const double tol_abs = p.tolerance * (bnorm > 0.0 ? bnorm : 1.0);
@@ -1181,54 +1312,12 @@ SolveStats fgmres(const BsrView& A, const double* vals, const double* b, double*
         k_second_sweep_col<double, double><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc.ptr, K.V.ptr, n, K.w.ptr, K.Z.ptr, n, st);
         GOAL_CHECK_LAUNCH();
       }
+    } else if (p.precision == PREC_MIXED) {
+      issue_inner(A, n, mi, sweep2, st, sti, K, inner_arrays(K, (__half*)nullptr));
+    } else if (p.precision == PREC_MIXED_F32) {
+      issue_inner(A, n, mi, sweep2, st, sti, K, inner_arrays(K, (float*)nullptr));
     } else {
-      // inner GMRES in the dof-scaled space (FP32 vectors, A^ = S A S in
-      // binary16) with the right preconditioner, fixed mi iterations:
-      // Z_j = S M^-1 V16 y with V16 the inner basis (binary16) started from S V_j
-      k_col_to_f32<<<nbx, 256, 0, s>>>(n, K.V.ptr, n, st, K.sd.ptr, K.r32.ptr);
-      GOAL_CHECK_LAUNCH();
-      k_norm2_part<float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, red32);
-      GOAL_CHECK_LAUNCH();
-      k_cycle_fin<float><<<1, 256, 0, s>>>(nbx, red32, sti, gin, mi, nullptr);
-      GOAL_CHECK_LAUNCH();
-      k_gate<<<1, 1, 0, s>>>(st, sti);
-      GOAL_CHECK_LAUNCH();
-      k_scale_into<__half, float><<<nbx, 256, 0, s>>>(n, K.r32.ptr, sti, K.V16.ptr);
-      GOAL_CHECK_LAUNCH();
-      // r32 = D^-1 v_0; later steps get D^-1 v_it from the normalization
-      k_bj_colin<float, __half><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.V16.ptr, n, sti, K.r32.ptr);
-      GOAL_CHECK_LAUNCH();
-      for (int it = 0; it < mi; ++it) {
-        // z = M^-1 v_it (in t32 with the second sweep, else r32); w32 = A^ z
-        float* z = K.r32.ptr;
-        if (sweep2) {
-          k_spmv_sweep<float, __half, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr,
-                                                                           K.Bc32.ptr, K.V16.ptr, n, sti, K.t32.ptr);
-          GOAL_CHECK_LAUNCH();
-          z = K.t32.ptr;
-        }
-        k_spmv_col<float, __half><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, z, 0, sti, K.w32.ptr);
-        GOAL_CHECK_LAUNCH();
-        // orthogonalize, normalize into v_{it+1}, and r32 = D^-1 v_{it+1}
-        arnoldi_orth<float, __half>(n, K.V16.ptr, K.w32.ptr, sti, Hin, mi + 1, csin, snin, gin, dots32, red32, mi, 0.0,
-                                    kInnerPasses, s, K.Dinv32.ptr, K.r32.ptr);
-      }
-      k_backsolve<float><<<1, 32, 0, s>>>(sti, Hin, mi + 1, gin, yin);
-      GOAL_CHECK_LAUNCH();
-      k_combine<__half, float><<<nbx, 256, 0, s>>>(n, K.V16.ptr, n, yin, sti, K.w32.ptr, 1);
-      GOAL_CHECK_LAUNCH();
-      k_bj<float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Dinv32.ptr, K.w32.ptr, K.r32.ptr);
-      GOAL_CHECK_LAUNCH();
-      if (sweep2) {
-        k_spmv<float, __half, false><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, K.A16.ptr, K.r32.ptr, nullptr,
-                                                                   K.t32.ptr);
-        GOAL_CHECK_LAUNCH();
-        k_second_sweep_col<float, float><<<grid_for(n, 256), 256, 0, s>>>(N, K.Bc32.ptr, K.w32.ptr, 0, K.t32.ptr,
-                                                                   K.r32.ptr, 0, nullptr);
-        GOAL_CHECK_LAUNCH();
-      }
-      k_f32_to_col<<<nbx, 256, 0, s>>>(n, K.r32.ptr, K.sd.ptr, K.Z.ptr, n, st);
-      GOAL_CHECK_LAUNCH();
+      issue_inner(A, n, mi, sweep2, st, sti, K, inner_arrays(K, (double*)nullptr));
     }
     k_spmv_col<double, double><<<spmv_grid(N), 256, 0, s>>>(N, A.brow_ptr, A.bcol, vals, K.Z.ptr, n, st, K.w.ptr);
     GOAL_CHECK_LAUNCH();

@@ -28,6 +28,11 @@ struct Mechanics {
   Disc* disc = nullptr;
   int model = MODEL_NEOHOOKEAN;
   bool stabilization = true;
+  // J2 state writes at elastic points: false is goal's behaviour
+  // (src/goal_J2.cpp:97-136 writes Fp only where the point yields, so the Fp
+  // of an earlier plastic Newton iterate survives at points that end elastic,
+  // and States::update commits it); true writes Fp = Fp_old there.
+  bool fp_reset = false;
   std::vector<MaterialRow> mats_h;
   DevBuf<double> mats;      // per set: kappa, mu, K, Y, c0, 1/kappa, c0/(2 mu), 1/(16 kappa)
   DevBuf<double> U;         // 4N nodal solution: u_x u_y u_z p per node (the DOF layout)
@@ -51,6 +56,7 @@ struct SolInfo {
   Mpnn* learned = nullptr;  // network used when a solve asks for the learned preconditioner
   DevBuf<double> R, dMdu;   // 4N
   DevBuf<double> A;         // 16 x nnzb, block (n,m) row-major
+  DevBuf<double> csr;       // nnz: A in the order of the scalar CSR graph, written on request
   void init(Disc* d);
 };
 

@@ -87,6 +87,18 @@ class Disc {
     col_idx.resize(get_nnz());
     check(goal_disc_get_graph(h_, row_ptr.data(), col_idx.data()));
   }
+  // the same graph as device pointers owned by the disc (plus the 4x4-block graph)
+  struct DeviceGraph {
+    const int* brow_ptr = nullptr;
+    const int* bcol = nullptr;
+    const int* row_ptr = nullptr;
+    const int* col_idx = nullptr;
+  };
+  DeviceGraph device_graph() const {
+    DeviceGraph g;
+    check(goal_disc_device_graph(h_, &g.brow_ptr, &g.bcol, &g.row_ptr, &g.col_idx));
+    return g;
+  }
   // lid of equation eq of node n (src/goal_disc.cpp:195-201)
   static long long get_lid(long long node, int eq) { return node * 4 + eq; }
   goal_disc handle() const { return h_; }
@@ -123,6 +135,12 @@ class Mechanics {
     return U;
   }
   void set_solution(const std::vector<double>& U) { check(goal_mechanics_set_solution(h_, U.data())); }
+  // the u and p fields on the device (4 per node)
+  double* device_solution() const {
+    double* U = nullptr;
+    check(goal_mechanics_device_solution(h_, &U));
+    return U;
+  }
   void update_states() { check(goal_states_update(h_)); }  // States::update
   goal_mechanics handle() const { return h_; }
 
@@ -144,6 +162,23 @@ class SolInfo {
   std::vector<double> dRdu() const {  // CSR values in the order of Disc::get_owned_graph
     std::vector<double> v(disc_.get_nnz());
     check(goal_sol_info_get_dRdu_csr(h_, v.data()));
+    return v;
+  }
+  // owned->R, owned->dMdu and dRdu (4x4 blocks) as device pointers owned by the SolInfo
+  struct DeviceView {
+    double* R = nullptr;
+    double* dMdu = nullptr;
+    double* bsr = nullptr;
+  };
+  DeviceView device_view() const {
+    DeviceView v;
+    check(goal_sol_info_device_view(h_, &v.R, &v.dMdu, &v.bsr));
+    return v;
+  }
+  // dRdu in the order of Disc::device_graph().row_ptr/col_idx (device, refreshed by this call)
+  double* device_dRdu() const {
+    double* v = nullptr;
+    check(goal_sol_info_device_csr(h_, &v));
     return v;
   }
   goal_sol_info handle() const { return h_; }

@@ -1,5 +1,13 @@
-"""Reader for the discretization inputs goal loads: a serial SCOREC SMB v5 mesh,
-its ``.dmg`` model and the association file (src/goal_disc.cpp:28-120).
+"""Reader for the discretization inputs goal loads: a SCOREC SMB v5 mesh (one
+part file, or the part files of a partitioned mesh), its ``.dmg`` model and
+the association file (src/goal_disc.cpp:28-120).
+
+File names follow SCOREC's convention: a mesh file ``name.smb`` is stored as
+part files ``name0.smb``, ``name1.smb``, ... (one per MPI rank of the run that
+wrote it; ``cube.smb`` of the reference's 3D test is ``cube0.smb`` to
+``cube3.smb``, and ``cube-serial.smb`` is ``cube-serial0.smb``). Every part
+is read and the parts are joined into one mesh: part-boundary vertices appear
+in every part that holds them, with the same coordinates, and are merged.
 
 Only what the element path needs is decoded: vertex coordinates, tets (from
 the tet->triangle->edge->vertex downward chain) and the (model tag, model dim)
@@ -19,6 +27,7 @@ depend on the numbering).
 """
 from __future__ import annotations
 
+import os
 import struct
 from typing import Dict, List, Tuple
 
@@ -60,7 +69,14 @@ def read_smb(path: str):
     coords = np.frombuffer(data, dtype=">f8", count=3 * nv, offset=off).astype(np.float64).reshape(nv, 3)
     off += 8 * 3 * nv
     off += 8 * 2 * nv  # parametric coordinates of vertices (unused)
-    off += 4           # remote-copy count of a serial part (zero)
+    # remote copies: the number of peer parts, their ids, the number of
+    # vertices shared with each, then those vertices' local ids (zero peers
+    # in a one-part mesh); the join matches shared vertices by coordinates
+    npeers = int(ints(1)[0])
+    if npeers:
+        ints(npeers)
+        shared = ints(npeers)
+        ints(int(shared.sum()))
     cls = {}
     for t, n in ((_SMB_VERT, nv), (_SMB_EDGE, ne), (_SMB_TRI, nt), (_SMB_TET, ntet)):
         cls[t] = ints(2 * n).reshape(n, 2)
@@ -125,11 +141,22 @@ def read_assoc(path: str) -> List[Tuple[str, str, List[Tuple[int, int]]]]:
     return out
 
 
-def load(geom_file: str, mesh_file: str, assoc_file: str) -> Mesh:
-    coords, edges, tris, tets, cls = read_smb(mesh_file)
-    _, up = read_dmg(geom_file)
-    assoc = read_assoc(assoc_file)
+def part_files(mesh_file: str) -> List[str]:
+    """The part files of a mesh file name: ``name.smb`` itself if it exists,
+    else ``name0.smb``, ``name1.smb``, ... as far as they exist."""
+    if os.path.exists(mesh_file):
+        return [mesh_file]
+    stem = mesh_file[:-4] if mesh_file.endswith(".smb") else mesh_file
+    out = []
+    while os.path.exists(f"{stem}{len(out)}.smb"):
+        out.append(f"{stem}{len(out)}.smb")
+    if not out:
+        raise FileNotFoundError(f"no SMB part files for {mesh_file} ({stem}0.smb, ...)")
+    return out
 
+
+def _vertices(coords, edges, tris, tets):
+    """Vertices of every triangle (from its edges) and tet (from its triangles)."""
     tri_verts = np.empty((tris.shape[0], 3), np.int64)
     for t in range(tris.shape[0]):
         vs = []
@@ -148,6 +175,49 @@ def load(geom_file: str, mesh_file: str, assoc_file: str) -> Mesh:
         if len(vs) != 4:
             raise ValueError("degenerate tet in SMB file")
         tet_verts[t] = vs
+    return tri_verts, tet_verts
+
+
+def read_parts(mesh_file: str):
+    """Reads every part of a mesh and joins them: (coords, tri_verts,
+    tet_verts, vertex / triangle / tet classification). Vertices shared by
+    parts are merged by coordinates; triangles on part boundaries are kept once."""
+    coords_all, vcls_all, tri_all, tcls_all, tet_all, ecls_all = [], [], [], [], [], []
+    key_to_id: Dict[Tuple[float, float, float], int] = {}
+    seen_tris = set()
+    for path in part_files(mesh_file):
+        coords, edges, tris, tets, cls = read_smb(path)
+        tri_verts, tet_verts = _vertices(coords, edges, tris, tets)
+        gid = np.empty(coords.shape[0], np.int64)
+        for v in range(coords.shape[0]):
+            key = tuple(coords[v])
+            g = key_to_id.get(key)
+            if g is None:
+                g = len(coords_all)
+                key_to_id[key] = g
+                coords_all.append(coords[v])
+                vcls_all.append(cls[_SMB_VERT][v])
+            gid[v] = g
+        for t in range(tri_verts.shape[0]):
+            g = gid[tri_verts[t]]
+            k = tuple(sorted(g))
+            if k in seen_tris:
+                continue
+            seen_tris.add(k)
+            tri_all.append(g)
+            tcls_all.append(cls[_SMB_TRI][t])
+        tet_all.append(gid[tet_verts])
+        ecls_all.append(cls[_SMB_TET])
+    coords = np.array(coords_all, dtype=np.float64).reshape(-1, 3)
+    cls = {_SMB_VERT: np.array(vcls_all).reshape(-1, 2), _SMB_TRI: np.array(tcls_all).reshape(-1, 2),
+           _SMB_TET: np.concatenate(ecls_all).reshape(-1, 2)}
+    return coords, np.array(tri_all, np.int64).reshape(-1, 3), np.concatenate(tet_all).reshape(-1, 4), cls
+
+
+def load(geom_file: str, mesh_file: str, assoc_file: str) -> Mesh:
+    coords, tri_verts, tet_verts, cls = read_parts(mesh_file)
+    _, up = read_dmg(geom_file)
+    assoc = read_assoc(assoc_file)
     tet_verts = orient_positive(coords, tet_verts.astype(np.int32))
 
     def closure_up(dim, tag):
@@ -162,7 +232,7 @@ def load(geom_file: str, mesh_file: str, assoc_file: str) -> Mesh:
         return seen
 
     elem_set_names: List[str] = []
-    elem_set = np.full(tets.shape[0], -1, np.int32)
+    elem_set = np.full(tet_verts.shape[0], -1, np.int32)
     node_sets: Dict[str, np.ndarray] = {}
     side_sets: Dict[str, np.ndarray] = {}
     vcls = cls[_SMB_VERT]
@@ -173,12 +243,12 @@ def load(geom_file: str, mesh_file: str, assoc_file: str) -> Mesh:
             idx = len(elem_set_names)
             elem_set_names.append(name)
             c = cls[_SMB_TET]
-            for t in range(tets.shape[0]):
+            for t in range(tet_verts.shape[0]):
                 if (int(c[t, 1]), int(c[t, 0])) in ents_set:
                     elem_set[t] = idx
         elif kind == "side set":
             c = cls[_SMB_TRI]
-            sel = [t for t in range(tris.shape[0]) if (int(c[t, 1]), int(c[t, 0])) in ents_set]
+            sel = [t for t in range(tri_verts.shape[0]) if (int(c[t, 1]), int(c[t, 0])) in ents_set]
             side_sets[name] = np.ascontiguousarray(tri_verts[sel], dtype=np.int32).reshape(-1, 3)
         else:
             sel = [v for v in range(coords.shape[0]) if vclosure[v] & ents_set]

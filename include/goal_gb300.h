@@ -188,6 +188,14 @@ int goal_mechanics_get_solution(goal_mechanics m, double* U);
 /* DWR weights for the error chain: z_diff and z_coarse, 4*num_nodes each
  * (u_z_diff/p_z_diff and p_z_coarse, src/goal_nested_adjoint.cpp:52-72) */
 int goal_mechanics_set_weights(goal_mechanics m, const double* z_diff, const double* z_coarse);
+/* J2 state writes at points that end a Newton solve elastic. 0 (default) is
+ * goal's behaviour: J2::at_point writes Fp only where the point yields
+ * (src/goal_J2.cpp:97-136), so the Fp of an earlier plastic Newton iterate
+ * survives at a point that ends elastic and States::update commits it as
+ * Fp_old. 1 also writes Fp = Fp_old at elastic points, so the committed state
+ * is the converged iterate's. No counterpart in the reference: an option for
+ * load paths on which goal's behaviour stops Newton from converging. */
+int goal_mechanics_set_fp_reset(goal_mechanics m, int on);
 /* state fields; sigma/Fp/Fp_old: 9*num_elems, eqps/eqps_old: num_elems */
 int goal_states_set(goal_mechanics m, int which, const double* values);
 int goal_states_get(goal_mechanics m, int which, double* values);
@@ -206,6 +214,37 @@ int goal_sol_info_set_vector(goal_sol_info s, int which, const double* values);
 int goal_sol_info_get_dRdu_csr(goal_sol_info s, double* values);
 int goal_sol_info_get_dRdu_bsr(goal_sol_info s, double* values);
 int goal_sol_info_destroy(goal_sol_info s);
+
+/* ---------------------------------------------------------------- device views
+ * The linear objects as DEVICE pointers owned by the handles, for callers
+ * whose own solver or vectors live on the GPU (goal's SolInfo hands out
+ * owned->R, owned->dMdu and owned->dRdu, src/goal_sol_info.hpp:12-16,29; its
+ * Tpetra objects are the ones Belos and MueLu read, src/goal_linear_solve.cpp:72-90).
+ * No copies: the arrays are the ones goal_assemble, the boundary conditions
+ * and goal_solve_device read and write, on the discretization's stream
+ * (goal_disc_stream), so order other streams against it. They stay valid until
+ * the handle is destroyed. Any output pointer may be NULL.
+ *
+ * goal_disc_device_graph: the block graph (brow_ptr[num_nodes+1],
+ * bcol[nnzb], sorted; the matrix of 4x4 blocks, block k row-major at
+ * bsr_vals + 16k) and goal's scalar CSR graph (row_ptr[num_dofs+1],
+ * col_idx[nnz], the same arrays goal_disc_get_graph copies out; Disc's owned
+ * graph, src/goal_disc.cpp:307-332). The scalar graph is built on the device
+ * at the first request for it (one allocation, GOAL_ERR_CAPACITY beyond 2^31-1
+ * nonzeros). */
+int goal_disc_device_graph(goal_disc d, const int** brow_ptr, const int** bcol, const int** row_ptr,
+                           const int** col_idx);
+/* R[num_dofs], dMdu[num_dofs] and dRdu as 4x4 blocks (bsr_vals[16*nnzb]). */
+int goal_sol_info_device_view(goal_sol_info s, double** R, double** dMdu, double** bsr_vals);
+/* dRdu in the order of the scalar CSR graph (csr_vals[nnz]): written from the
+ * blocks by this call (a snapshot of the current matrix; call it again after
+ * the next assembly) into a buffer the SolInfo owns (allocated on the first
+ * call). Returns when the values are written. */
+int goal_sol_info_device_csr(goal_sol_info s, double** csr_vals);
+/* the nodal solution U[num_dofs] (u_x, u_y, u_z, p per node) that every
+ * assembly reads: the u and p fields of the mechanics, which Disc::add_soln
+ * updates after a linear solve (src/goal_disc.cpp:398-422) */
+int goal_mechanics_device_solution(goal_mechanics m, double** U);
 
 /* ---------------------------------------------------------------- assemble
  * assemble(Evaluators, SolInfo*) (src/goal_assembly.cpp:65-88) for the chains
@@ -260,8 +299,11 @@ int goal_set_tbcs(goal_mechanics m, goal_sol_info s, goal_bcs b, double t, int e
 /* ---------------------------------------------------------------- linear solve
  * goal::solve(params, A, x, b, disc) (src/goal_linear_solve.cpp:72-90) with
  * A = dRdu of the SolInfo. precision: 0 = FP64 FGMRES with block-Jacobi;
- * 1 = FP64 FGMRES whose preconditioner is inner_iters FP32 GMRES iterations
- * (FP32 matrix and block-Jacobi). precond: 0 = block-Jacobi, 1 = learned
+ * 1, 2, 3 = FP64 FGMRES (FP64 residual and update) whose preconditioner is
+ * inner_iters GMRES iterations with block-Jacobi on the dof-scaled matrix
+ * S A S, S = diag(|a_ii|^-1/2): 1 = matrix and Krylov basis stored in
+ * binary16, FP32 arithmetic; 2 = stored in FP32, FP32 arithmetic; 3 = FP64
+ * storage and arithmetic (nested FP64). precond: 0 = block-Jacobi, 1 = learned
  * block-Jacobi correction (see goal_learned_*), falling back to plain
  * block-Jacobi when the outer iterations exceed learned_cap.
  * Convergence: ||b - A x||_2 <= tolerance ||b||_2. */
@@ -375,9 +417,10 @@ int goal_learned_destroy(goal_learned l);
  * U (4 per node: u_x, u_y, u_z, p). The value is written to the device double
  * *J on `stream` (a cudaStream_t; NULL = the default stream); the call does not
  * wait for it. It performs kernel launches only: no device allocation, no
- * free, no synchronisation. For callers that may not allocate: code running
- * inside a stream capture, and frameworks that hand all free device memory to
- * their own pool. The partial sums live in a fixed 128 KiB device array of this
+ * free, no synchronisation. It is for callers that may not allocate device
+ * memory: a framework that hands all free device memory to its own pool (a
+ * cudaMalloc there fails or steals from that pool), or a time-critical loop
+ * that must not pay for an allocation. The partial sums live in a fixed 128 KiB device array of this
  * library, which limits a call to 16,777,216 elements (GOAL_ERR_CAPACITY
  * beyond). The first call on each device, with that device current, looks up
  * that array's address; make it before any stream capture. Nothing has to be

@@ -309,6 +309,12 @@ struct Args {
   double* qoi_value;     // 1
   int* num_plastic;      // 1
   int* status;           // 1: 0 ok, 1 return-map failure
+  // 1 = also write Fp = Fp_old at elastic points. 0 is goal's behaviour
+  // (src/goal_J2.cpp:97-136 writes Fp only where the point yields, so an
+  // earlier Newton iterate's plastic Fp survives at points that end elastic
+  // and States::update commits it); 1 is the option that makes the committed
+  // state the converged iterate's.
+  int fp_elastic_reset;
 };
 
 // ---------------------------------------------------------------- von Mises
@@ -480,6 +486,8 @@ int eval_element(const Args& A, int e, double ks_max, double ks_scale, ElemOut<T
       }
     } else {
       if (A.save && A.eqps_out) A.eqps_out[e] = val(eqps);
+      if (A.save && A.Fp_out && A.fp_elastic_reset)
+        for (int k = 0; k < 9; ++k) A.Fp_out[9 * e + k] = A.Fp_old[9 * e + k];
     }
     T pm = 0.5 * kappa * (J - 1.0 / J);
     for (int k = 0; k < 9; ++k) sigma.a[k] = s.a[k] / J + pm * I.a[k];

@@ -64,7 +64,7 @@ class _Args(ctypes.Structure):
         ("sigma_out", ctypes.c_void_p), ("Fp_out", ctypes.c_void_p), ("eqps_out", ctypes.c_void_p),
         ("R", ctypes.c_void_p), ("row_ptr", ctypes.c_void_p), ("col_idx", ctypes.c_void_p),
         ("vals", ctypes.c_void_p), ("dMdu", ctypes.c_void_p), ("qoi_value", ctypes.c_void_p),
-        ("num_plastic", ctypes.c_void_p), ("status", ctypes.c_void_p),
+        ("num_plastic", ctypes.c_void_p), ("status", ctypes.c_void_p), ("fp_elastic_reset", ctypes.c_int),
     ]
 
 
@@ -172,9 +172,12 @@ def assemble(mesh, model: int, mats: List[Material], u: np.ndarray, p: np.ndarra
              qoi: int = QOI_NONE, rho: float = 0.0,
              graph: Optional[Tuple[np.ndarray, np.ndarray]] = None,
              R: Optional[np.ndarray] = None, vals: Optional[np.ndarray] = None, dMdu: Optional[np.ndarray] = None,
-             error_weights: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None, threads: bool = False):
+             error_weights: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None, threads: bool = False,
+             fp_reset: bool = False):
     """One assemble(E, SolInfo*) of a chain; accumulates into R / vals / dMdu.
-    Returns (qoi value, number of plastic points)."""
+    ``fp_reset`` also writes Fp = Fp_old at elastic points (goal keeps the
+    last plastic iterate's Fp there). Returns (qoi value, number of plastic
+    points)."""
     L = lib()
     mats_arr = np.array([m.row() for m in mats], dtype=np.float64)
     u = np.ascontiguousarray(u, dtype=np.float64)
@@ -192,6 +195,7 @@ def assemble(mesh, model: int, mats: List[Material], u: np.ndarray, p: np.ndarra
     a.mode = mode
     a.fad = int(fad)
     a.save = int(save)
+    a.fp_elastic_reset = int(fp_reset)
     a.qoi = qoi
     a.rho = rho
     if error_weights is not None:
@@ -293,6 +297,7 @@ class Problem:
     stabilization: bool = True
     qoi: int = QOI_AVG_DISP
     rho: float = 0.0
+    fp_reset: bool = False   # Fp = Fp_old at elastic points (not goal's behaviour)
 
 
 class Primal:
@@ -315,7 +320,7 @@ class Primal:
         vals = np.zeros(len(self.graph[1]))
         dMdu = np.zeros(self.n)
         assemble(pr.mesh, pr.model, pr.mats, self.u, self.p, self.states, mode=PRIMAL, fad=True, save=True,
-                 stabilization=pr.stabilization, graph=self.graph, R=R, vals=vals, dMdu=dMdu)
+                 stabilization=pr.stabilization, graph=self.graph, R=R, vals=vals, dMdu=dMdu, fp_reset=pr.fp_reset)
         apply_tbcs(pr.mesh, pr.tbcs, t_now, R)
         apply_dbcs(pr.mesh, pr.dbcs, t_now, self.u, R, self.graph, vals, dMdu, jac=True)
         return R, vals
@@ -324,7 +329,7 @@ class Primal:
         pr = self.prob
         R = np.zeros(self.n)
         assemble(pr.mesh, pr.model, pr.mats, self.u, self.p, self.states, mode=PRIMAL, fad=False, save=True,
-                 stabilization=pr.stabilization, R=R)
+                 stabilization=pr.stabilization, R=R, fp_reset=pr.fp_reset)
         apply_tbcs(pr.mesh, pr.tbcs, t_now, R)
         apply_dbcs(pr.mesh, pr.dbcs, t_now, self.u, R)
         return R

@@ -1,7 +1,8 @@
 """Generates the golden fixtures under tests/golden/ from the reference tree.
 
-Run in a container that has the reference mounted:
-    python tests/golden/make_golden.py /root/reference
+Run in a container that has the reference checked out; its root directory is
+the one required argument:
+    python tests/golden/make_golden.py <reference root>
 
 * cube_mesh.npz   -- the reference's 3D test mesh (test/mesh/cube/cube-serial0.smb
   with cube.dmg and cube.txt), decoded by goal_gb300.smb into coordinates,
@@ -9,9 +10,15 @@ Run in a container that has the reference mounted:
 * regression.json -- the regression QoI values the reference's examples assert
   (src/goal_regression.cpp:14-23) for the 3D cases on that mesh, with the
   inputs of each YAML file restated as data.
+* goal_inputs/    -- the reference's own input files for those cases, copied
+  byte for byte with the directory layout their relative paths expect:
+  example/primal/{neohookean_uniaxial_3D,J2_uniaxial_3D,J2_traction_3D}.yaml
+  and test/mesh/cube/{cube.dmg, cube.txt, cube0..3.smb (the 4-part mesh the
+  YAML files name as cube.smb), cube-serial0.smb}.
 """
 import json
 import os
+import shutil
 import sys
 
 import numpy as np
@@ -58,5 +65,16 @@ def main(ref):
                        cases=cases), f, indent=1)
 
 
+    inputs = os.path.join(HERE, "goal_inputs")
+    for rel in ["example/primal/neohookean_uniaxial_3D.yaml", "example/primal/J2_uniaxial_3D.yaml",
+                "example/primal/J2_traction_3D.yaml", "test/mesh/cube/cube.dmg", "test/mesh/cube/cube.txt",
+                "test/mesh/cube/cube-serial0.smb"] + [f"test/mesh/cube/cube{k}.smb" for k in range(4)]:
+        dst = os.path.join(inputs, rel)
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        shutil.copyfile(os.path.join(ref, rel), dst)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference root>")
+    main(sys.argv[1])

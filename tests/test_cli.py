@@ -87,6 +87,60 @@ def test_cli_primal_regression(case, tmp_path, monkeypatch):
     assert any("regression" in l for l in lines)
 
 
+GOAL_INPUTS = os.path.join(ROOT, "tests", "golden", "goal_inputs")
+REFERENCE_CASES = ["neohookean_uniaxial_3D", "J2_uniaxial_3D", "J2_traction_3D"]
+
+
+def _reference_yaml(case):
+    return os.path.join(GOAL_INPUTS, "example", "primal", f"{case}.yaml")
+
+
+@pytest.mark.parametrize("case", REFERENCE_CASES)
+def test_reference_input_files_load(case):
+    """The reference's own example files, unchanged: the YAML parses with the
+    keys the driver accepts, and the mesh it names (cube.smb: the 4-part
+    SCOREC mesh cube0.smb .. cube3.smb, joined) is the reference's serial test
+    mesh with the same node, side and element sets."""
+    import numpy as np
+    from goal_gb300 import cli, smb
+    _, p = cli._problem(_reference_yaml(case))  # (J2_traction_3D.yaml's list is named "J2 uniaxial 3D")
+    assert p["regression"]["value"] == _cases()[case]["value"]
+    base = os.path.dirname(_reference_yaml(case))
+    dp = p["discretization"]
+    assert dp["mesh file"] == "../../test/mesh/cube/cube.smb"
+    joined = smb.load(cli._resolve(base, dp["geom file"]), cli._resolve(base, dp["mesh file"]),
+                      cli._resolve(base, dp["assoc file"]))
+    cube = os.path.join(GOAL_INPUTS, "test", "mesh", "cube")
+    serial = smb.load(os.path.join(cube, "cube.dmg"), os.path.join(cube, "cube-serial0.smb"),
+                      os.path.join(cube, "cube.txt"))
+    assert (joined.num_nodes, joined.num_elems) == (serial.num_nodes, serial.num_elems) == (51, 132)
+
+    def tets(m):
+        return sorted(tuple(sorted(map(tuple, m.coords[t]))) for t in m.tets)
+
+    assert tets(joined) == tets(serial)
+    for k in serial.node_sets:
+        assert sorted(map(tuple, joined.coords[joined.node_sets[k]])) == sorted(map(tuple, serial.coords[serial.node_sets[k]]))
+    for k in serial.side_sets:
+        assert np.asarray(joined.side_sets[k]).shape == np.asarray(serial.side_sets[k]).shape
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", REFERENCE_CASES)
+def test_cli_primal_on_reference_input_files(case, tmp_path, monkeypatch):
+    """GoalPrimal (src/main_primal.cpp:68-90) on the reference's example file
+    itself, byte for byte: its mesh, boundary conditions, material, Newton
+    settings and regression check (src/goal_regression.cpp:14-23) pass."""
+    from goal_gb300 import cli
+    monkeypatch.chdir(tmp_path)  # output files land in the working directory, as in goal
+    lines = []
+    J = cli.primal(_reference_yaml(case), out=lines.append)
+    c = _cases()[case]
+    assert abs(J - c["value"]) < c["tolerance"]
+    assert sum(l.startswith(" > J(uH) = ") for l in lines) == c["num_steps"]
+    assert any(l.startswith(" > regression: ") for l in lines)
+
+
 def _with_output(text, **opts):
     extra = "".join(f"    {k}: {v}\n" for k, v in opts.items())
     return text.replace("  output:\n", "  output:\n" + extra)
