@@ -32,7 +32,8 @@ class NewtonStats(ctypes.Structure):
     """goal_newton_stats"""
     _fields_ = [("iters", ctypes.c_int), ("converged", ctypes.c_int), ("linear_iters", ctypes.c_int),
                 ("inner_iters", ctypes.c_int), ("norms", ctypes.c_double * 32),
-                ("seconds_assembly", ctypes.c_double), ("seconds_solve", ctypes.c_double)]
+                ("seconds_assembly", ctypes.c_double), ("seconds_solve", ctypes.c_double),
+                ("backtracks", ctypes.c_int)]
 
 
 class DwrResult(ctypes.Structure):

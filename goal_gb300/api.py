@@ -139,6 +139,10 @@ class Mechanics:
         if fp_reset:
             check(lib().goal_mechanics_set_fp_reset(self.h, 1))
 
+    def set_line_search(self, max_halvings: int):
+        """Newton backtracking for goal_primal_solve (0: goal's full steps)."""
+        check(lib().goal_mechanics_set_line_search(self.h, int(max_halvings)))
+
     def set_solution(self, U: np.ndarray):
         U = _f64(U).reshape(-1)
         assert U.size == self.disc.num_dofs
@@ -316,7 +320,7 @@ def primal_solve(mech: Mechanics, s: SolInfo, bcs: Bcs, t_now: float, t_old: flo
                                  ctypes.byref(params or solve_params()), ctypes.byref(st))
     out = dict(iters=st.iters, converged=bool(st.converged), linear_iters=st.linear_iters,
                inner_iters=st.inner_iters, norms=list(st.norms[:min(st.iters, 32)]),
-               seconds_assembly=st.seconds_assembly, seconds_solve=st.seconds_solve)
+               seconds_assembly=st.seconds_assembly, seconds_solve=st.seconds_solve, backtracks=st.backtracks)
     if rc != 0:
         try:
             check(rc)

@@ -195,6 +195,13 @@ int goal_assembly_timing(int enable) {
   GOAL_API_END
 }
 
+int goal_set_element_buffer_limit(long long bytes) {
+  GOAL_API_BEGIN
+  GOAL_ARG(bytes >= 0, "goal_set_element_buffer_limit: negative size");
+  goal::set_element_buffer_limit(bytes);
+  GOAL_API_END
+}
+
 int goal_assembly_timing_read(double* ms, long long* count) {
   GOAL_API_BEGIN
   GOAL_ARG(ms && count, "null argument");
@@ -416,6 +423,13 @@ int goal_mechanics_set_fp_reset(goal_mechanics m, int on) {
   GOAL_API_BEGIN
   GOAL_ARG(m, "goal_mechanics_set_fp_reset: null handle");
   m->m->fp_reset = on != 0;
+  GOAL_API_END
+}
+
+int goal_mechanics_set_line_search(goal_mechanics m, int max_halvings) {
+  GOAL_API_BEGIN
+  GOAL_ARG(m && max_halvings >= 0 && max_halvings <= 30, "goal_mechanics_set_line_search: bad arguments");
+  m->m->line_search = max_halvings;
   GOAL_API_END
 }
 
@@ -686,9 +700,11 @@ int goal_primal_solve(goal_mechanics m, goal_sol_info s, goal_bcs b, double t_no
   p.max_iters = max_iters;
   p.tolerance = tolerance;
   p.lin = to_params(lin);
+  p.line_search = m->m->line_search;
   static thread_local Krylov K;
   NewtonStats r = primal_solve(*m->m, *s->s, b->dbcs, b->tbcs, t_now, t_old, p, K);
   if (stats) {
+    stats->backtracks = r.backtracks;
     stats->iters = r.iters;
     stats->converged = r.converged;
     stats->linear_iters = r.linear_iters;

@@ -114,6 +114,15 @@ __global__ void k_diag(int N, const int* brow_ptr, const int* bcol, int* diag) {
   }
 }
 
+// btr[k] = index of block (m, n) for block k = (n, m) of the symmetric block graph
+__global__ void k_block_transpose(int N, const int* brow_ptr, const int* bcol, int* btr) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
+    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
+      const int m = bcol[k], b = brow_ptr[m];
+      btr[k] = b + lower_bound_dev(bcol + b, brow_ptr[m + 1] - b, n);
+    }
+}
+
 // Jones-Plassmann round with first-fit colours. Reads colours of the previous
 // round only (cin), so the result does not depend on scheduling.
 __global__ void k_color_round(int E, const int* tets, const int* ne_ptr, const int* ne_list,
@@ -497,6 +506,13 @@ void Disc::csr_graph(int* row_ptr_h, int* col_idx_h) const {
   rp.download(row_ptr_h, stream);
   ci.download(col_idx_h, stream);
   GOAL_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Disc::block_transpose_map() {
+  if (btr.ptr) return;
+  btr.alloc(nnzb);
+  k_block_transpose<<<grid_for(num_nodes, 256), 256, 0, stream>>>(num_nodes, brow_ptr.ptr, bcol.ptr, btr.ptr);
+  GOAL_CHECK_LAUNCH();
 }
 
 void Disc::csr_graph_device() {

@@ -102,11 +102,15 @@ struct Disc {
   // the scalar CSR graph kept on the device (4N+1 row pointers, nnz columns),
   // built on the first request for device pointers
   DevBuf<int> csr_row_ptr, csr_col_idx;
+  // btr[k]: index of block (m, n) for block k = (n, m); built by the first
+  // transposed (ADJOINT) assembly
+  DevBuf<int> btr;
 
   void build();                // Disc::build_data: graph, colouring, geometry
   DiscView view() const;
   void csr_graph(int* row_ptr, int* col_idx) const;  // host outputs
   void csr_graph_device();     // fills csr_row_ptr / csr_col_idx once
+  void block_transpose_map();  // fills btr once
 };
 
 // Builds the uniformly refined nested mesh of ``base`` on the device

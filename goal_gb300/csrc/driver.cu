@@ -18,6 +18,11 @@ __global__ void k_add(long long n, double* U, const double* du) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     U[i] += du[i];
 }
+// U = U0 + a du (a line-search trial from the iteration's starting point)
+__global__ void k_axpy_from(long long n, double* U, const double* U0, double a, const double* du) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    U[i] = fma(a, du[i], U0[i]);
+}
 
 // compensated dot product partials (also used for norms)
 __global__ void k_dot_part(long long n, const double* a, const double* b, double* part) {
@@ -177,10 +182,21 @@ NewtonStats primal_solve(Mechanics& m, SolInfo& s, const std::vector<DBC>& dbcs,
   cudaStream_t st = m.disc->stream;
   K.stream = st;
   const long long n = 4ll * m.disc->num_nodes;
-  DevBuf<double> du;
+  DevBuf<double> du, U0;
   du.alloc(n);
+  if (p.line_search > 0) U0.alloc(n);
   int iter = 1;
   bool converged = false;
+  Chain cr;
+  cr.mode = MODE_PRIMAL;
+  cr.jacobian = 0;
+  cr.save_states = 1;
+  auto residual_norm = [&]() {
+    assemble(m, &s, cr, nullptr, st);
+    apply_tbcs(m, s, tbcs, t_now, nullptr, st);
+    apply_dbcs(m, s, dbcs, t_now, false, st);
+    return std::sqrt(device_dot(n, s.R.ptr, s.R.ptr, m.red, st));
+  };
   while (iter <= p.max_iters && !converged) {
     double t0 = now();
     Chain cj;
@@ -190,6 +206,8 @@ NewtonStats primal_solve(Mechanics& m, SolInfo& s, const std::vector<DBC>& dbcs,
     assemble(m, &s, cj, nullptr, st);
     apply_tbcs(m, s, tbcs, t_now, nullptr, st);
     apply_dbcs(m, s, dbcs, t_now, true, st);
+    // ||R|| at the iteration's starting point (the line search's reference)
+    const double norm0 = p.line_search > 0 ? std::sqrt(device_dot(n, s.R.ptr, s.R.ptr, m.red, st)) : 0.0;
     k_axpy_neg<<<grid_for(n, 256), 256, 0, st>>>(n, s.R.ptr);
     GOAL_CHECK_LAUNCH();
     du.zero(st);
@@ -199,16 +217,23 @@ NewtonStats primal_solve(Mechanics& m, SolInfo& s, const std::vector<DBC>& dbcs,
     out.inner_iters += ls.inner_iters;
     out.last = ls;
     double t2 = now();
-    k_add<<<grid_for(n, 256), 256, 0, st>>>(n, m.U.ptr, du.ptr);
-    GOAL_CHECK_LAUNCH();
-    Chain cr;
-    cr.mode = MODE_PRIMAL;
-    cr.jacobian = 0;
-    cr.save_states = 1;
-    assemble(m, &s, cr, nullptr, st);
-    apply_tbcs(m, s, tbcs, t_now, nullptr, st);
-    apply_dbcs(m, s, dbcs, t_now, false, st);
-    double norm = std::sqrt(device_dot(n, s.R.ptr, s.R.ptr, m.red, st));
+    double norm = 0.0;
+    if (p.line_search > 0) {
+      GOAL_CUDA(cudaMemcpyAsync(U0.ptr, m.U.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      double a = 1.0;
+      for (int h = 0;; ++h) {
+        k_axpy_from<<<grid_for(n, 256), 256, 0, st>>>(n, m.U.ptr, U0.ptr, a, du.ptr);
+        GOAL_CHECK_LAUNCH();
+        norm = residual_norm();
+        if (norm < (1.0 - 1e-4 * a) * norm0 || h >= p.line_search) break;
+        a *= 0.5;
+        out.backtracks++;
+      }
+    } else {
+      k_add<<<grid_for(n, 256), 256, 0, st>>>(n, m.U.ptr, du.ptr);
+      GOAL_CHECK_LAUNCH();
+      norm = residual_norm();
+    }
     double t3 = now();
     out.seconds_assembly += (t1 - t0) + (t3 - t2);
     out.seconds_solve += t2 - t1;

@@ -16,6 +16,10 @@ struct NewtonParams {
   int max_iters = 5;           // "nonlinear max iters"
   double tolerance = 1e-8;     // "nonlinear tolerance" (absolute ||R||_2)
   SolveParams lin;
+  // 0: goal's full Newton steps. k > 0: backtracking on ||R||_2, the step
+  // U += a du with the first a in 1, 1/2, ..., 2^-k whose residual norm is
+  // below (1 - 1e-4 a) times the iteration's starting norm (else the smallest)
+  int line_search = 0;
 };
 
 struct NewtonStats {
@@ -24,6 +28,7 @@ struct NewtonStats {
   double norms[32] = {0};
   int linear_iters = 0;
   int inner_iters = 0;
+  int backtracks = 0;          // halvings of the step taken by the line search
   double seconds_assembly = 0.0;
   double seconds_solve = 0.0;
   SolveStats last;

@@ -64,6 +64,7 @@ struct ElemArgs {
   double* ebuf;    // two-phase mode: per element [R (16) | 16 blocks x 16] (stride estride)
   double* dbuf;    // two-phase mode: per element dM/du (16)
   int estride;
+  int ebase;       // element slot of the buffers' first entry (a chunk's first element)
   int begin, end;
   int stab, save, overwrite, qoi;
   int fp_reset;    // also write Fp = Fp_old at elastic points (goal leaves Fp as it was)
@@ -123,7 +124,13 @@ __device__ bool exp_traceless_sym(const double A[3][3], double out[3][3]) {
 
 // BUF: element outputs go to the per-element buffer (phase 1 of the two-phase
 // assembly) instead of being accumulated in place by one colour at a time.
-template <int MODEL, int MODE, bool JAC, bool ERR, bool BUF>
+// DSUM (with BUF): of the four diagonal element blocks (a, a) only column 3
+// (K^up_a, K^pp_aa) is formed and stored, packed in the block's first four
+// slots. The u columns of a matrix row sum to zero over the row's blocks (the
+// gradients of a linear tet's shape functions sum to zero, and every u column
+// of K^uu and K^pu is linear in them), so k_gather_diag forms the diagonal
+// blocks' u columns as negated sums of the off-diagonal blocks.
+template <int MODEL, int MODE, bool JAC, bool ERR, bool BUF, bool DSUM = false>
 __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   const int s = a.begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.end) return;
@@ -222,7 +229,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   // J2 radial return (closed form of goal's scalar Newton loop)
   double gamma = 1.0;
   bool plastic = false;
-  double smag = 0.0, mubar = 0.0, fyield = 0.0, k0 = 0.0, cc = 1.0, kh = 0.0, Xr = 0.0;
+  double smag = 0.0, mubar = 0.0, fyield = 0.0, k0 = 0.0, cc = 1.0, kh = 0.0, Xr = 0.0, rsmag = 0.0, rcc = 1.0;
   const double sq23 = 0.81649658092772603273;  // sqrt(2/3)
   if (MODEL == MODEL_J2 || (a.qoi == QOI_KS_VM)) {
     smag = sqrt(s00 * s00 + s11 * s11 + s22 * s22 + 2.0 * (s01 * s01 + s12 * s12 + s02 * s02));
@@ -234,8 +241,11 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
     fyield = smag - k0;
     if (fyield > 1.0e-12) {
       plastic = true;
+      // reciprocals formed once (a division costs several FP64 instructions)
+      rsmag = 1.0 / smag;
+      const double r2mu = 1.0 / (2.0 * mubar);
       // first Newton iterate of src/goal_J2.cpp:101-121 (H = 0 in the first slope)
-      double X1 = -(fyield / (-2.0 * mubar * 1.0));
+      double X1 = fyield * r2mu;
       double alpha1 = eq_old + sq23 * X1;
       double R1 = smag - (2.0 * mubar * X1 + sq23 * (Yld + Kh * alpha1));
       double r1 = fabs(R1);
@@ -243,13 +253,19 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       bool conv1 = (r1 < 1.0e-11) || (r1 < 1.0e-11 * Yld) || (r1 < 1.0e-11 * fyield);
       kh = conv1 ? 0.0 : (2.0 / 3.0) * Kh;
       cc = 2.0 * mubar + kh;
-      Xr = conv1 ? X1 : fyield / cc;
-      gamma = 1.0 - 2.0 * mubar * Xr / smag;
+      if (!conv1) {
+        rcc = 1.0 / cc;
+        Xr = fyield * rcc;
+      } else {
+        rcc = r2mu;  // cc = 2 mubar
+        Xr = X1;
+      }
+      gamma = 1.0 - 2.0 * mubar * Xr * rsmag;
       if (!(Xr >= 0.0) || !isfinite(Xr)) atomicOr(a.status, 1);
       if (a.save) {
         a.eqps[s] = eq_old + sq23 * Xr;
         // Fp = exp(dgam N) Fp_old (stored only at plastic points)
-        const double is = Xr / smag;
+        const double is = Xr * rsmag;
         const double Am[3][3] = {{s00 * is, s01 * is, s02 * is}, {s01 * is, s11 * is, s12 * is},
                                  {s02 * is, s12 * is, s22 * is}};
         double Ex[3][3];
@@ -372,7 +388,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       }
     }
     if constexpr (BUF) {
-      double* eb = a.ebuf + (size_t)s * a.estride;
+      double* eb = a.ebuf + (size_t)(s - a.ebase) * a.estride;
 #pragma unroll
       for (int n = 0; n < 4; ++n) st4(eb + 4 * n, Ru[n][0], Ru[n][1], Ru[n][2], Rp[n]);
     } else {
@@ -421,11 +437,11 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   double vq = 0.0, vh = 0.0, vn = 0.0;
   const bool need_n = plastic || (a.qoi == QOI_KS_VM);
   if (plastic) {
-    const double A1 = 2.0 * fyield * kh / (cc * cc * smag);
-    const double A2 = 2.0 * mubar * k0 / (cc * smag * smag);
+    const double A1 = 2.0 * fyield * kh * (rcc * rcc) * rsmag;
+    const double A2 = 2.0 * mubar * k0 * rcc * (rsmag * rsmag);
     yq = -A1 * (2.0 * alpha / 3.0);
     yh = A2 * (2.0 / 3.0) * smag;
-    yn = -A2 * (2.0 * alpha / smag);
+    yn = -A2 * (2.0 * alpha * rsmag);
   }
   if (a.qoi == QOI_KS_VM) {
     // dsmag_b = -2/3 smag h_b + 2 alpha/smag n_b ; dmubar_b = 2 alpha/3 q_b
@@ -470,7 +486,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
         for (int k = 0; k < 3; ++k)
           d[k] = c1 * (vq * qv[b][k] + vh * hv[b][k] + vn * nv[b][k] - gs * hv[b][k]);
       }
-      if constexpr (BUF) st4(a.dbuf + 16ll * s + 4 * b, d[0], d[1], d[2], 0.0);
+      if constexpr (BUF) st4(a.dbuf + 16ll * (s - a.ebase) + 4 * b, d[0], d[1], d[2], 0.0);
       else acc4(a.dMdu + 4 * v[b], (fm >> (16 + b)) & 1u, d[0], d[1], d[2], 0.0);
     }
   }
@@ -504,8 +520,14 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
     const double pu1 = twv[ai] - pu0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      const double cab = fma(CG[0], G[b][0], fma(CG[1], G[b][1], CG[2] * G[b][2]));
       const double eab = hv[ai][0] * hv[b][0] + hv[ai][1] * hv[b][1] + hv[ai][2] * hv[b][2];
+      if constexpr (DSUM) {
+        if (ai == b) {  // resolved at compile time (both loops unrolled)
+          st4(a.ebuf + (size_t)(s - a.ebase) * a.estride + 16 + 16 * (4 * ai + b), up0, up1, up2, fma(tJVs, eab, ppc));
+          continue;
+        }
+      }
+      const double cab = fma(CG[0], G[b][0], fma(CG[1], G[b][1], CG[2] * G[b][2]));
       double K[4][4];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -521,7 +543,7 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       for (int k = 0; k < 3; ++k) K[3][k] = fma(pu1, hv[b][k], -fma(eab, tvv[k], twv[b] * hv[ai][k]));
       K[3][3] = fma(tJVs, eab, ppc);
       if constexpr (BUF) {
-        double* eb = a.ebuf + (size_t)s * a.estride + 16 + 16 * (4 * ai + b);
+        double* eb = a.ebuf + (size_t)(s - a.ebase) * a.estride + 16 + 16 * (4 * ai + b);
 #pragma unroll
         for (int r = 0; r < 4; ++r) st4(eb + 4 * r, K[r][0], K[r][1], K[r][2], K[r][3]);
       } else if (MODE == MODE_PRIMAL) {
@@ -621,12 +643,20 @@ __global__ void k_fill_identity(int E, double* Fp) {
 }
 
 template <int MODEL, int MODE, bool JAC, bool ERR>
-void launch_colours(const Disc& d, ElemArgs args, cudaStream_t st, bool buffered) {
+void launch_colours(const Disc& d, ElemArgs args, cudaStream_t st, bool buffered, bool dsum = false) {
   const int block = 128;
   if (MODE == MODE_NONE || buffered) {
-    args.begin = 0;
-    args.end = d.num_elems;
-    k_elem<MODEL, MODE, JAC, ERR, true><<<(d.num_elems + block - 1) / block, block, 0, st>>>(args);
+    // elements [args.begin, args.end) into the buffer (all of them, or a chunk)
+    const int n = args.end - args.begin;
+    if (n <= 0) return;
+    if constexpr (JAC && MODE != MODE_NONE) {
+      if (dsum) {
+        k_elem<MODEL, MODE, JAC, ERR, true, true><<<(n + block - 1) / block, block, 0, st>>>(args);
+        GOAL_CHECK_LAUNCH();
+        return;
+      }
+    }
+    k_elem<MODEL, MODE, JAC, ERR, true><<<(n + block - 1) / block, block, 0, st>>>(args);
     GOAL_CHECK_LAUNCH();
   } else {
   for (int c = 0; c < d.num_colors; ++c) {
@@ -641,7 +671,7 @@ void launch_colours(const Disc& d, ElemArgs args, cudaStream_t st, bool buffered
 }
 
 template <int MODEL>
-void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t st, bool buf) {
+void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t st, bool buf, bool dsum) {
   if (c.error_chain) {
     GOAL_REQUIRE(!c.jacobian && c.mode == MODE_PRIMAL, GOAL_ERR_ARG, "the error chain is a residual (PRIMAL) chain");
     launch_colours<MODEL, MODE_PRIMAL, false, true>(d, args, st, buf);
@@ -651,11 +681,11 @@ void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t 
     if (c.jacobian) launch_colours<MODEL, MODE_NONE, true, false>(d, args, st, true);
     else launch_colours<MODEL, MODE_NONE, false, false>(d, args, st, true);
   } else if (c.mode == MODE_PRIMAL) {
-    if (c.jacobian) launch_colours<MODEL, MODE_PRIMAL, true, false>(d, args, st, buf);
+    if (c.jacobian) launch_colours<MODEL, MODE_PRIMAL, true, false>(d, args, st, buf, dsum);
     else launch_colours<MODEL, MODE_PRIMAL, false, false>(d, args, st, buf);
   } else {
     GOAL_REQUIRE(c.jacobian, GOAL_ERR_ARG, "ADJOINT mode is a Jacobian (FADT) chain");
-    launch_colours<MODEL, MODE_ADJOINT, true, false>(d, args, st, buf);
+    launch_colours<MODEL, MODE_ADJOINT, true, false>(d, args, st, buf, dsum);
   }
 }
 
@@ -663,8 +693,8 @@ void dispatch(const Disc& d, const Chain& c, const ElemArgs& args, cudaStream_t 
 // element buffer; TRANSPOSE reads column r of the transposed element block.
 template <bool TRANSPOSE>
 __device__ __forceinline__ void load_contrib(const double* __restrict__ ebuf, int estride, int v, int r, double& x0,
-                                             double& x1, double& x2, double& x3) {
-  const int s = v >> 4, lb = v & 15;
+                                             double& x1, double& x2, double& x3, int lo = 0) {
+  const int s = (v >> 4) - lo, lb = v & 15;
   if (TRANSPOSE) {
     const int lt = ((lb & 3) << 2) | (lb >> 2);
     const double* p = ebuf + (size_t)s * estride + 16 + 16 * lt + r;
@@ -713,19 +743,96 @@ __global__ void __launch_bounds__(256) k_gather_blocks(int count, const int* __r
   }
 }
 
+// k_gather_blocks for one chunk of elements [lo, hi) (the element buffer
+// holds that chunk only): the contributions of the chunk, in element order,
+// are added to the block as it stands, so chunk after chunk the additions
+// are the ones of the one-pass gather, in the same order.
+template <bool TRANSPOSE>
+__global__ void __launch_bounds__(256) k_gather_blocks_chunk(int count, const int* __restrict__ ks,
+                                                             const int* __restrict__ bptr,
+                                                             const int* __restrict__ blist,
+                                                             const double* __restrict__ ebuf, int estride,
+                                                             double* __restrict__ A, int accumulate, int lo, int hi) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4ll * count;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int k = __ldg(ks + (t >> 2)), r = (int)(t & 3);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (accumulate) ld4(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+    const int c1 = __ldg(bptr + k + 1);
+    for (int c = __ldg(bptr + k); c < c1; ++c) {
+      const int v = __ldg(blist + c), e = v >> 4;
+      if (e < lo || e >= hi) continue;
+      double x0, x1, x2, x3;
+      load_contrib<TRANSPOSE>(ebuf, estride, v, r, x0, x1, x2, x3, lo);
+      a0 += x0; a1 += x1; a2 += x2; a3 += x3;
+    }
+    st4(A + 16ll * k + 4 * r, a0, a1, a2, a3);
+  }
+}
+
+// Phase 2 for the diagonal blocks after a DSUM element phase, once the
+// off-diagonal blocks are gathered: thread (node n, row r). PRIMAL: the u
+// columns of row r are the negated sum of row r of the row's off-diagonal
+// blocks; column 3 sums the elements' packed column-3 contributions in element
+// order. TRANSPOSE (ADJOINT mode stores dR/du^T): rows 0..2 are the negated
+// sums of the same rows of the blocks (m, n) of the block column (btr), row 3
+// sums the packed contributions. No atomics; fixed order.
+template <bool TRANSPOSE>
+__global__ void __launch_bounds__(256) k_gather_diag(int N, const int* __restrict__ brow_ptr,
+                                                     const int* __restrict__ diag, const int* __restrict__ btr,
+                                                     const int* __restrict__ bptr, const int* __restrict__ blist,
+                                                     const double* __restrict__ ebuf, int estride,
+                                                     double* __restrict__ A) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4ll * N;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(t >> 2), r = (int)(t & 3);
+    const int kd = __ldg(diag + n), k0 = __ldg(brow_ptr + n), k1 = __ldg(brow_ptr + n + 1);
+    const int c0 = __ldg(bptr + kd), c1 = __ldg(bptr + kd + 1);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (!TRANSPOSE || r < 3) {
+      for (int k = k0; k < k1; ++k) {
+        if (k == kd) continue;
+        const int kk = TRANSPOSE ? __ldg(btr + k) : k;
+        double x0, x1, x2, x3;
+        ld4(A + 16ll * kk + 4 * r, x0, x1, x2, x3);
+        a0 -= x0; a1 -= x1; a2 -= x2;
+        if (TRANSPOSE) a3 -= x3;
+      }
+    }
+    if (!TRANSPOSE) {
+      for (int c = c0; c < c1; ++c) {
+        const int v = __ldg(blist + c);
+        a3 += __ldg(ebuf + (size_t)(v >> 4) * estride + 16 + 16 * (v & 15) + r);
+      }
+    } else if (r == 3) {
+      for (int c = c0; c < c1; ++c) {
+        const int v = __ldg(blist + c);
+        double x0, x1, x2, x3;
+        ld4(ebuf + (size_t)(v >> 4) * estride + 16 + 16 * (v & 15), x0, x1, x2, x3);
+        a0 += x0; a1 += x1; a2 += x2; a3 += x3;
+      }
+    }
+    st4(A + 16ll * kd + 4 * r, a0, a1, a2, a3);
+  }
+}
+
 // Phase 2 for nodal vectors: node n, row q sums the element rows of its
 // incident elements (entries 4*s + a of nlist) in element order.
+// [lo, hi): the element slots the buffer holds (a chunk; the buffer's first
+// entry is slot lo); the one-pass gather has lo = 0, hi = E.
 __global__ void __launch_bounds__(256) k_gather_nodes(int N, const int* __restrict__ nptr,
                                                       const int* __restrict__ nlist, const double* __restrict__ ebuf,
-                                                      int estride, double* __restrict__ out, int accumulate) {
+                                                      int estride, double* __restrict__ out, int accumulate, int lo,
+                                                      int hi) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4ll * N;
        t += (long long)gridDim.x * blockDim.x) {
     const int n = (int)(t >> 2), q = (int)(t & 3);
     double acc = accumulate ? out[t] : 0.0;
     const int c1 = __ldg(nptr + n + 1);
     for (int c = __ldg(nptr + n); c < c1; ++c) {
-      const int v = __ldg(nlist + c);
-      acc += __ldg(ebuf + (size_t)(v >> 2) * estride + 4 * (v & 3) + q);
+      const int v = __ldg(nlist + c), e = v >> 2;
+      if (e < lo || e >= hi) continue;
+      acc += __ldg(ebuf + (size_t)(e - lo) * estride + 4 * (v & 3) + q);
     }
     out[t] = acc;
   }
@@ -849,6 +956,19 @@ void assembly_timing_read(double* ms, long long* count) {
   *count = g_phase.count;
 }
 
+namespace {
+long long g_ebuf_limit = 0;  // bytes; 0 = a quarter of the device's memory
+}
+
+void set_element_buffer_limit(long long bytes) { g_ebuf_limit = bytes < 0 ? 0 : bytes; }
+
+long long element_buffer_limit() {
+  if (g_ebuf_limit > 0) return g_ebuf_limit;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || total_b == 0) return 8ll << 30;
+  return (long long)(total_b / 4);
+}
+
 double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w, cudaStream_t st) {
   const Disc& d = *m.disc;
   ElemArgs a;
@@ -896,46 +1016,79 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
   }
   const bool buf = !c.colored && (c.mode != MODE_NONE || c.jacobian);
   const bool scatter = c.mode != MODE_NONE;
+  const int E = d.num_elems;
+  int chunk = E;  // elements per pass of the two-phase assembly
   if (buf) {
     a.estride = c.jacobian ? 272 : 16;
-    size_t need = (size_t)d.num_elems * a.estride;
+    const size_t per_elem = sizeof(double) * (a.estride + ((c.jacobian && c.qoi != QOI_NONE) ? 16 : 0));
+    chunk = (int)std::max<long long>(1, std::min<long long>(E, element_buffer_limit() / per_elem));
+    size_t need = (size_t)chunk * a.estride;
     if (m.ebuf.n < need) m.ebuf.alloc(need);
     a.ebuf = m.ebuf.ptr;
     if (c.jacobian && c.qoi != QOI_NONE) {
-      if (m.dbuf.n < 16ull * d.num_elems) m.dbuf.alloc(16ull * d.num_elems);
+      if (m.dbuf.n < 16ull * chunk) m.dbuf.alloc(16ull * chunk);
       a.dbuf = m.dbuf.ptr;
     }
   }
+  // diagonal blocks from row sums: buffered Jacobian chains that overwrite, in one pass
+  const bool dsum = buf && scatter && c.jacobian && c.overwrite && chunk == E;
+  if (dsum && c.mode == MODE_ADJOINT) const_cast<Disc&>(d).block_transpose_map();
   const bool timed = g_phase.on;
   if (timed) GOAL_CUDA(cudaEventRecord(g_phase.ev[0], st));
-  if (m.model == MODEL_J2) dispatch<MODEL_J2>(d, c, a, st, buf);
-  else dispatch<MODEL_NEOHOOKEAN>(d, c, a, st, buf);
-  if (timed) GOAL_CUDA(cudaEventRecord(g_phase.ev[1], st));
-  if (buf && scatter) {
-    const int acc = c.overwrite ? 0 : 1;
-    k_gather_nodes<<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(d.num_nodes, d.nptr.ptr, d.nlist.ptr,
-                                                                        m.ebuf.ptr, a.estride, s->R.ptr, acc);
-    GOAL_CHECK_LAUNCH();
-    if (c.jacobian) {
-      const int noff = d.nnzb - d.num_nodes;
-      const int* lists[2] = {d.offd.ptr, d.diag.ptr};
-      const int counts[2] = {noff, d.num_nodes};
-      for (int q = 0; q < 2; ++q) {
-        if (counts[q] <= 0) continue;
-        if (c.mode == MODE_ADJOINT)
-          k_gather_blocks<true><<<grid_for(4ll * counts[q], 256), 256, 0, st>>>(
-              counts[q], lists[q], d.bptr.ptr, d.blist.ptr, m.ebuf.ptr, a.estride, s->A.ptr, acc);
-        else
-          k_gather_blocks<false><<<grid_for(4ll * counts[q], 256), 256, 0, st>>>(
-              counts[q], lists[q], d.bptr.ptr, d.blist.ptr, m.ebuf.ptr, a.estride, s->A.ptr, acc);
-        GOAL_CHECK_LAUNCH();
+  for (int e0 = 0; e0 < E; e0 += chunk) {
+    const int e1 = buf ? std::min(E, e0 + chunk) : E;
+    a.begin = e0;
+    a.end = e1;
+    a.ebase = e0;
+    if (m.model == MODEL_J2) dispatch<MODEL_J2>(d, c, a, st, buf, dsum);
+    else dispatch<MODEL_NEOHOOKEAN>(d, c, a, st, buf, dsum);
+    if (timed && e0 == 0) GOAL_CUDA(cudaEventRecord(g_phase.ev[1], st));
+    if (!buf) break;  // the coloured path covers every element itself
+    const int acc = (c.overwrite && e0 == 0) ? 0 : 1;
+    const bool chunked = chunk < E;
+    if (scatter) {
+      k_gather_nodes<<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(d.num_nodes, d.nptr.ptr, d.nlist.ptr,
+                                                                          m.ebuf.ptr, a.estride, s->R.ptr, acc, e0, e1);
+      GOAL_CHECK_LAUNCH();
+      if (c.jacobian) {
+        const int noff = d.nnzb - d.num_nodes;
+        const int* lists[2] = {d.offd.ptr, d.diag.ptr};
+        const int counts[2] = {noff, d.num_nodes};
+        for (int q = 0; q < 2; ++q) {
+          if (counts[q] <= 0) continue;
+          const int g = grid_for(4ll * counts[q], 256);
+          if (q == 1 && dsum) {  // the diagonal blocks, after the off-diagonal ones
+            if (c.mode == MODE_ADJOINT)
+              k_gather_diag<true><<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(
+                  d.num_nodes, d.brow_ptr.ptr, d.diag.ptr, d.btr.ptr, d.bptr.ptr, d.blist.ptr, m.ebuf.ptr,
+                  a.estride, s->A.ptr);
+            else
+              k_gather_diag<false><<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(
+                  d.num_nodes, d.brow_ptr.ptr, d.diag.ptr, nullptr, d.bptr.ptr, d.blist.ptr, m.ebuf.ptr,
+                  a.estride, s->A.ptr);
+          } else if (chunked) {
+            if (c.mode == MODE_ADJOINT)
+              k_gather_blocks_chunk<true><<<g, 256, 0, st>>>(counts[q], lists[q], d.bptr.ptr, d.blist.ptr, m.ebuf.ptr,
+                                                             a.estride, s->A.ptr, acc, e0, e1);
+            else
+              k_gather_blocks_chunk<false><<<g, 256, 0, st>>>(counts[q], lists[q], d.bptr.ptr, d.blist.ptr,
+                                                              m.ebuf.ptr, a.estride, s->A.ptr, acc, e0, e1);
+          } else if (c.mode == MODE_ADJOINT) {
+            k_gather_blocks<true><<<g, 256, 0, st>>>(counts[q], lists[q], d.bptr.ptr, d.blist.ptr, m.ebuf.ptr,
+                                                     a.estride, s->A.ptr, acc);
+          } else {
+            k_gather_blocks<false><<<g, 256, 0, st>>>(counts[q], lists[q], d.bptr.ptr, d.blist.ptr, m.ebuf.ptr,
+                                                      a.estride, s->A.ptr, acc);
+          }
+          GOAL_CHECK_LAUNCH();
+        }
       }
     }
-  }
-  if (buf && c.jacobian && c.qoi != QOI_NONE && s) {
-    k_gather_nodes<<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(d.num_nodes, d.nptr.ptr, d.nlist.ptr, m.dbuf.ptr,
-                                                                        16, s->dMdu.ptr, c.overwrite ? 0 : 1);
-    GOAL_CHECK_LAUNCH();
+    if (c.jacobian && c.qoi != QOI_NONE && s) {
+      k_gather_nodes<<<grid_for(4ll * d.num_nodes, 256), 256, 0, st>>>(d.num_nodes, d.nptr.ptr, d.nlist.ptr,
+                                                                          m.dbuf.ptr, 16, s->dMdu.ptr, acc, e0, e1);
+      GOAL_CHECK_LAUNCH();
+    }
   }
   if (timed) GOAL_CUDA(cudaEventRecord(g_phase.ev[2], st));
   int hstat = 0;

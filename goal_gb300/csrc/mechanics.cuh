@@ -33,6 +33,7 @@ struct Mechanics {
   // of an earlier plastic Newton iterate survives at points that end elastic,
   // and States::update commits it); true writes Fp = Fp_old there.
   bool fp_reset = false;
+  int line_search = 0;      // Newton backtracking halvings (0: goal's full Newton steps)
   std::vector<MaterialRow> mats_h;
   DevBuf<double> mats;      // per set: kappa, mu, K, Y, c0, 1/kappa, c0/(2 mu), 1/(16 kappa)
   DevBuf<double> U;         // 4N nodal solution: u_x u_y u_z p per node (the DOF layout)
@@ -79,6 +80,11 @@ struct ErrorWeights {
 // assemble(E, SolInfo*) (src/goal_assembly.cpp:65-88) for one chain.
 // Returns the QoI value when chain.qoi != QOI_NONE.
 double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w, cudaStream_t stream);
+// Size cap of the two-phase assembly's element buffer: a mesh whose buffer
+// would be larger is assembled in chunks of elements (same sums, same order).
+// 0 restores the default, a quarter of the device's memory.
+void set_element_buffer_limit(long long bytes);
+long long element_buffer_limit();
 // Device time of the element-kernel phase and of the gather phase of every
 // assemble() while enabled (enable clears the sums).
 void assembly_timing(bool enable);

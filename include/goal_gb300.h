@@ -272,6 +272,14 @@ typedef struct {
   int colored; /* 0: element buffer + deterministic gather (default); 1: colour-by-colour in place */
 } goal_chain;
 int goal_assemble(goal_mechanics m, goal_sol_info s, const goal_chain* chain, double* qoi_value);
+/* No counterpart in the reference. Size cap in bytes of the per-element buffer
+ * of the default scatter (272 doubles per element for a Jacobian chain, 2176
+ * bytes; 16 more with a QoI). A mesh whose buffer would be larger is
+ * assembled in chunks of elements, each evaluated into the buffer and then
+ * added to the matrix and vectors; the sums and their order are those of one
+ * pass, so the results are the same bits. 0 (default) = a quarter of the
+ * device's memory. Process-wide. */
+int goal_set_element_buffer_limit(long long bytes);
 /* No counterpart in the reference. Device time of goal_assemble's two phases,
  * measured with CUDA events on the discretization's stream: enable != 0 clears
  * the sums and starts measuring, 0 stops. ms[0] = element kernel(s), ms[1] =
@@ -347,9 +355,16 @@ typedef struct {
   double norms[32];
   double seconds_assembly;
   double seconds_solve;
+  int backtracks; /* step halvings of the line search (goal_mechanics_set_line_search) */
 } goal_newton_stats;
 int goal_primal_solve(goal_mechanics m, goal_sol_info s, goal_bcs b, double t_now, double t_old, int max_iters,
                       double tolerance, const goal_solve_params* lin, goal_newton_stats* stats);
+/* No counterpart in the reference (goal takes full Newton steps). max_halvings
+ * > 0 makes goal_primal_solve backtrack: the step is U += a du with the first
+ * a in 1, 1/2, ..., 2^-max_halvings whose residual norm is below
+ * (1 - 1e-4 a) times the norm at the start of the iteration (else the
+ * smallest a). 0 (default) is goal's full step. */
+int goal_mechanics_set_line_search(goal_mechanics m, int max_halvings);
 
 /* ---------------------------------------------------------------- nested adjoint + DWR
  * NestedAdjoint (src/goal_nested_adjoint.cpp): build_data creates the uniformly

@@ -35,16 +35,19 @@ NEOHOOKEAN, J2 = 0, 1
 QOI_NONE, QOI_AVG_DISP, QOI_KS = 0, 1, 2
 
 
+TUNED_LIB = os.path.join(BUILD, "libtuned.so")
+
+
 def build(force: bool = False) -> str:
     """Compile the C++ restatement (plain g++, no FMA contraction, so x86 and
-    Arm hosts give the same bits)."""
+    Arm hosts give the same bits) and the tuned CPU baseline (tuned.cpp)."""
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "oracle.cpp")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
-               src, "-o", LIB + ".tmp"]
-        subprocess.check_call(cmd)
-        os.replace(LIB + ".tmp", LIB)
+    for src, lib, flags in ((os.path.join(HERE, "oracle.cpp"), LIB, ["-O2", "-ffp-contract=off"]),
+                            (os.path.join(HERE, "tuned.cpp"), TUNED_LIB, ["-O3"])):
+        if force or not os.path.exists(lib) or os.path.getmtime(lib) < os.path.getmtime(src):
+            cmd = ["g++", *flags, "-std=c++17", "-fPIC", "-shared", "-fopenmp", src, "-o", lib + ".tmp"]
+            subprocess.check_call(cmd)
+            os.replace(lib + ".tmp", lib)
     return LIB
 
 
@@ -509,3 +512,85 @@ def nested_adjoint(primal: Primal, t_now: float, t_old: float):
     return dict(nested=nested, graph=graph, A=A, R=R, dMdu=dMdu, z=z, eta=eta, bound=bound,
                 elem_err=elem_err, base_err=base_err, z_coarse=zc, z_diff=zd, Re=Re, u=u, p=p,
                 edges=edges, parent=parent)
+
+
+# ------------------------------------------------------------------ tuned CPU baseline
+class TunedAssembly:
+    """The "tuned" CPU baseline of the primal Jacobian assembly (tuned.cpp):
+    closed-form tangent, per-mesh geometry, coloured OpenMP scatter into 4x4
+    blocks. A baseline timed beside the GPU path, checked against the
+    dual-number restatement; not a checker itself."""
+
+    def __init__(self, mesh, model: int, mats: List[Material], Fp_old: np.ndarray, stabilization: bool = True):
+        build()
+        L = ctypes.CDLL(TUNED_LIB)
+        L.tuned_setup.restype = None
+        L.tuned_setup.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 5
+        L.tuned_color.restype = ctypes.c_int
+        L.tuned_color.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.tuned_assemble.restype = ctypes.c_int
+        L.tuned_assemble.argtypes = ([ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5 +
+                                     [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_longlong] + [ctypes.c_void_p] * 5)
+        self.L = L
+        self.mesh = mesh
+        self.model = model
+        self.stab = int(stabilization)
+        E, N = mesh.num_elems, mesh.num_nodes
+        self.tets = np.ascontiguousarray(mesh.tets, dtype=np.int32)
+        self.es = np.ascontiguousarray(mesh.elem_set, dtype=np.int32)
+        self.mats = np.array([m.row() for m in mats], dtype=np.float64)
+        self.Fp_old = np.ascontiguousarray(Fp_old, dtype=np.float64).reshape(E, 9)
+        self.geo = np.zeros((E, 14))
+        self.cpinv = np.zeros((E, 6))
+        coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+        L.tuned_setup(E, _p(coords), _p(self.tets), _p(self.Fp_old), _p(self.geo), _p(self.cpinv))
+        colors = np.zeros(E, np.int32)
+        self.ncolors = L.tuned_color(N, E, _p(self.tets), _p(colors))
+        if self.ncolors < 0:
+            raise RuntimeError("tuned_color: more than 128 colours")
+        self.order = np.ascontiguousarray(np.argsort(colors, kind="stable"), dtype=np.int32)
+        self.color_ptr = np.ascontiguousarray(np.searchsorted(colors[self.order], np.arange(self.ncolors + 1)),
+                                              dtype=np.int32)
+        # node graph and the 16 block indices of every element
+        a = np.repeat(self.tets, 4, axis=1).astype(np.int64)      # (E,16): node a of pair (a, b)
+        b = np.tile(self.tets, (1, 4)).astype(np.int64)           # node b
+        keys = a * N + b
+        uniq = np.unique(keys)
+        self.nnzb = len(uniq)
+        rows = uniq // N
+        self.brow_ptr = np.searchsorted(rows, np.arange(N + 1)).astype(np.int32)
+        self.bcol = (uniq % N).astype(np.int32)
+        self.blk = np.ascontiguousarray(np.searchsorted(uniq, keys), dtype=np.int32)
+        self.R = np.zeros(4 * N)
+        self.A = np.zeros(16 * self.nnzb)
+        self.sigma = np.zeros((E, 9))
+        self.Fp = self.Fp_old.copy()
+        self.eqps = np.zeros(E)
+
+    def assemble(self, U: np.ndarray, eqps_old: np.ndarray) -> int:
+        """One primal Jacobian assembly with state writes; returns the return-map failures."""
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
+        eq = np.ascontiguousarray(eqps_old, dtype=np.float64)
+        m = self.mesh
+        return self.L.tuned_assemble(m.num_nodes, m.num_elems, _p(self.tets), _p(self.es), _p(self.mats), self.model,
+                                     self.stab, _p(self.geo), _p(self.cpinv), _p(U), _p(self.Fp_old), _p(eq),
+                                     self.ncolors, _p(self.color_ptr), _p(self.order), _p(self.blk), self.nnzb,
+                                     _p(self.R), _p(self.A), _p(self.sigma), _p(self.Fp), _p(self.eqps))
+
+    def csr_values(self) -> np.ndarray:
+        """The blocks in the order of goal's scalar CSR graph (csr_graph)."""
+        N = self.mesh.num_nodes
+        deg = np.diff(self.brow_ptr)
+        out = np.empty(16 * self.nnzb)
+        Ab = self.A.reshape(-1, 4, 4)
+        pos = 0
+        for n in range(N):
+            k0, k1 = self.brow_ptr[n], self.brow_ptr[n + 1]
+            blk = Ab[k0:k1]                                       # (deg, 4, 4)
+            rows = np.transpose(blk, (1, 0, 2)).reshape(4, -1)    # row r: blocks side by side
+            out[pos:pos + rows.size] = rows.ravel()
+            pos += rows.size
+        assert pos == out.size and deg.sum() == self.nnzb
+        return out

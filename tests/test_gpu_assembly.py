@@ -255,7 +255,13 @@ def test_assembly_is_deterministic_and_overwrite_matches_accumulate(meshes, colo
     assert np.array_equal(R1, s.R) and np.array_equal(A1, s.dRdu_bsr())
     s.zero_all()
     api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, overwrite=False, colored=colored)
-    assert np.array_equal(R1, s.R) and np.array_equal(A1, s.dRdu_bsr())
+    assert np.array_equal(R1, s.R)
+    if colored:
+        assert np.array_equal(A1, s.dRdu_bsr())
+    else:
+        # accumulating sums every block from its element blocks; overwriting
+        # forms the diagonal blocks' u columns from the rows' off-diagonal blocks
+        assert np.abs(s.dRdu_bsr() - A1).max() <= 1e-13 * np.abs(A1).max()
     # both scatter strategies assemble the same matrix (up to summation order)
     api.assemble(m, s, api.PRIMAL, jacobian=True, save_states=False, colored=not colored)
     assert np.abs(s.dRdu_bsr() - A1).max() <= 1e-13 * np.abs(A1).max()
@@ -332,3 +338,32 @@ def test_measured_fp64_peak_is_plausible():
     v = ctypes.c_double()
     assert lib().goal_measure_fp64_peak(ctypes.byref(v)) == 0
     assert 0.5 < v.value < 2.0, v.value
+
+
+@pytest.mark.parametrize("mode", [api.PRIMAL, api.ADJOINT])
+def test_chunked_element_buffer_same_bits(mode):
+    """With the element buffer capped (goal_set_element_buffer_limit) the
+    two-phase assembly runs in chunks of elements; R, the matrix blocks and
+    dM/du are the same bits as one pass over all elements, and the one-pass
+    default (diagonal blocks formed from the rows' off-diagonal blocks) agrees
+    with both to 1e-13 of each row's largest entry."""
+    from goal_gb300 import lib
+    mesh = kuhn_cube(5)
+    u, p, st = random_state(mesh, 11, 1e-3, O.J2)
+    d, m, s = make_gpu(mesh, api.J2, u, p, st)
+    qoi = api.QOI_AVG_DISP if mode == api.ADJOINT else api.QOI_NONE
+    # one pass, every block summed from its element blocks (accumulating into zeros)
+    s.zero_all()
+    api.assemble(m, s, mode, jacobian=True, save_states=False, qoi=qoi, overwrite=False)
+    R1, A1, M1, C1 = s.R, s.dRdu_bsr(), s.dMdu, s.dRdu_csr()
+    # default: one pass, diagonal blocks from row sums
+    api.assemble(m, s, mode, jacobian=True, save_states=False, qoi=qoi)
+    C0 = s.dRdu_csr()
+    try:
+        assert lib().goal_set_element_buffer_limit(7 * 2304 * 8) == 0  # chunks of about 60 of the 750 elements
+        s2 = api.SolInfo(d)
+        api.assemble(m, s2, mode, jacobian=True, save_states=False, qoi=qoi)
+        assert np.array_equal(s2.R, R1) and np.array_equal(s2.dRdu_bsr(), A1) and np.array_equal(s2.dMdu, M1)
+    finally:
+        lib().goal_set_element_buffer_limit(0)
+    assert rel_rows(C0, C1, d.graph()[0]) <= 1e-13
