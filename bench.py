@@ -238,6 +238,13 @@ def cpu_tuned_rate(mesh, u, p, Fp_old, eqps_old, seconds):
     return mesh.num_elems * done / t_used, done
 
 
+def workload_config(n, mesh, nnz, frac, world):
+    """The workload's ``config`` object, the same for both arms."""
+    return {"workload": f"kuhn cube {n}^3 x 6 tets, J2 mixed u-p, primal R+J assembly",
+            "elements": mesh.num_elems, "nodes": mesh.num_nodes, "nnz": int(nnz), "yield_fraction": round(frac, 4),
+            "l2": "working set > L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -263,8 +270,7 @@ def run_reference(a):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "elem/s", "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1000.0 * wall / a.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"kuhn cube {a.n}^3 x 6 tets, J2 mixed u-p, primal R+J assembly",
-                   "elements": mesh.num_elems, "nodes": mesh.num_nodes, "yield_fraction": frac},
+        "config": workload_config(a.n, mesh, len(cache["g"][1]), frac, int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": value, "unit": "elem/s", "cores": threads, "kind": "port",
                          "sample": f"{elems} element evaluations over {a.steps} steps (bounded samples of the mesh), "
                                    f"dual-number Jacobian, OpenMP element loop + serial scatter"},
@@ -892,16 +898,13 @@ def main():
         "metric": METRIC, "value": value, "unit": "elem/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"kuhn cube {a.n}^3 x 6 tets, J2 mixed u-p, primal R+J assembly",
-                   "elements": E, "nodes": mesh.num_nodes, "nnz": d.nnz, "colors": d.num_colors,
-                   "yield_fraction": round(frac, 4), "l2": "working set > L2 (no flush)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(a.n, mesh, d.nnz, frac, world),
         "e2e": {"value": replica_value(E, e2e_ms, world), "unit": "elem/s", "h2d_bytes_per_step": 8 * 4 * mesh.num_nodes,
                 "d2h_bytes_per_step": 8 * 4 * mesh.num_nodes},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
-                     "kernel": "k_elem<J2, PRIMAL, Jacobian> (phase 1 of the assembly)",
+                     "kernel": "k_elem<J2, PRIMAL, Jacobian> (phase 1 of the assembly)", "colors": d.num_colors,
                      "kernel_ms": elem_ms, "gather_ms": gather_ms,
                      "algorithmic_bytes_per_step": alg, "algorithmic_bytes_per_element": alg / E,
                      "binding_roof": "fp64", "fp64": fp64},

@@ -44,8 +44,9 @@ __global__ void k_colors_orig(int E, const int* color, const int* orig, int* out
 
 }  // namespace
 
-void states_to_host(const Mechanics& m, int which, double* out) {
+void states_to_host(Mechanics& m, int which, double* out) {
   const Disc& d = *m.disc;
+  if (which == GOAL_STATE_FP) m.materialize_fp();
   const int E = d.num_elems;
   const double* src = nullptr;
   int nc = 9;
@@ -67,6 +68,9 @@ void states_to_host(const Mechanics& m, int which, double* out) {
 
 void states_from_host(Mechanics& m, int which, const double* in) {
   const Disc& d = *m.disc;
+  // pending plastic writes were formed with the current Fp_old: form them
+  // before any state changes (a new Fp replaces them)
+  m.materialize_fp();
   const int E = d.num_elems;
   double* dst = nullptr;
   int nc = 9;

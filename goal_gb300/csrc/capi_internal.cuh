@@ -5,7 +5,7 @@
 
 namespace goal {
 
-void states_to_host(const Mechanics& m, int which, double* out);
+void states_to_host(Mechanics& m, int which, double* out);
 void states_from_host(Mechanics& m, int which, const double* in);
 void bsr_to_csr(const SolInfo& s, double* out_host);
 

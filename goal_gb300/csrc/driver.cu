@@ -269,6 +269,7 @@ void NestedAdjoint::build(Mechanics& base_mech) {
 }
 
 void NestedAdjoint::refresh() {
+  base->materialize_fp();  // the children copy Fp
   const Disc& b = *base->disc;
   Disc& d = *disc;
   cudaStream_t st = d.stream;

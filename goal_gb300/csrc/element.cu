@@ -54,6 +54,8 @@ struct ElemArgs {
   double* sigma;
   double* Fp;
   double* eqps;
+  double* Apend;   // 6 x E deferred plastic increments (see StatesDev)
+  int* pend;
   double* R;
   double* A;
   double* dMdu;
@@ -264,24 +266,21 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
       if (!(Xr >= 0.0) || !isfinite(Xr)) atomicOr(a.status, 1);
       if (a.save) {
         a.eqps[s] = eq_old + sq23 * Xr;
-        // Fp = exp(dgam N) Fp_old (stored only at plastic points)
+        // Fp = exp(dgam N) Fp_old (stored only at plastic points): the
+        // increment dgam N is stored here, Fp formed when it is read
         const double is = Xr * rsmag;
-        const double Am[3][3] = {{s00 * is, s01 * is, s02 * is}, {s01 * is, s11 * is, s12 * is},
-                                 {s02 * is, s12 * is, s22 * is}};
-        double Ex[3][3];
-        if (!exp_traceless_sym(Am, Ex)) atomicOr(a.status, 2);
-        double Fo[3][3];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) Fo[q / 3][q % 3] = __ldg(a.Fp_old + q * E + s);
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int j = 0; j < 3; ++j)
-            a.Fp[(3 * i + j) * E + s] = Ex[i][0] * Fo[0][j] + Ex[i][1] * Fo[1][j] + Ex[i][2] * Fo[2][j];
+        a.Apend[0 * E + s] = s00 * is;
+        a.Apend[1 * E + s] = s11 * is;
+        a.Apend[2 * E + s] = s22 * is;
+        a.Apend[3 * E + s] = s01 * is;
+        a.Apend[4 * E + s] = s12 * is;
+        a.Apend[5 * E + s] = s02 * is;
+        a.pend[s] = 1;
       }
     } else if (a.save) {
       a.eqps[s] = eq_old;
       if (a.fp_reset) {
+        a.pend[s] = 0;
 #pragma unroll
         for (int q = 0; q < 9; ++q) a.Fp[q * E + s] = __ldg(a.Fp_old + q * E + s);
       }
@@ -637,6 +636,25 @@ __global__ void k_cpinv(int E, const double* Fp_old, double* Cpinv) {
   }
 }
 
+// Fp = exp(A) Fp_old at points with a pending plastic write (pend), then
+// pend = 0. Bit 2 of status: the exponential series did not settle.
+__global__ void k_materialize_fp(int E, const double* __restrict__ Apend, int* __restrict__ pend,
+                                 const double* __restrict__ Fp_old, double* __restrict__ Fp, int* status) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x) {
+    if (!pend[s]) continue;
+    const double a00 = Apend[0 * E + s], a11 = Apend[1 * E + s], a22 = Apend[2 * E + s];
+    const double a01 = Apend[3 * E + s], a12 = Apend[4 * E + s], a02 = Apend[5 * E + s];
+    const double Am[3][3] = {{a00, a01, a02}, {a01, a11, a12}, {a02, a12, a22}};
+    double Ex[3][3];
+    if (!exp_traceless_sym(Am, Ex)) atomicOr(status, 2);
+    double Fo[3][3];
+    for (int q = 0; q < 9; ++q) Fo[q / 3][q % 3] = Fp_old[q * E + s];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Fp[(3 * i + j) * E + s] = Ex[i][0] * Fo[0][j] + Ex[i][1] * Fo[1][j] + Ex[i][2] * Fo[2][j];
+    pend[s] = 0;
+  }
+}
+
 __global__ void k_fill_identity(int E, double* Fp) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < E; s += gridDim.x * blockDim.x)
     for (int q = 0; q < 9; ++q) Fp[q * E + s] = (q % 4 == 0) ? 1.0 : 0.0;
@@ -880,6 +898,9 @@ void Mechanics::init() {
   st.Fp.alloc(9ll * E);
   st.Fp_old.alloc(9ll * E);
   st.Cpinv.alloc(6ll * E);
+  st.Apend.alloc(6ll * E);
+  st.pend.alloc(E);
+  st.pend.zero(disc->stream);
   k_fill_identity<<<grid_for(E, 256), 256, 0, disc->stream>>>(E, st.Fp.ptr);
   k_fill_identity<<<grid_for(E, 256), 256, 0, disc->stream>>>(E, st.Fp_old.ptr);
   GOAL_CHECK_LAUNCH();
@@ -895,8 +916,21 @@ void Mechanics::refresh_cpinv() {
   GOAL_CHECK_LAUNCH();
 }
 
+void Mechanics::materialize_fp() {
+  const int E = disc->num_elems;
+  GOAL_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(int), disc->stream));
+  k_materialize_fp<<<grid_for(E, 256), 256, 0, disc->stream>>>(E, st.Apend.ptr, st.pend.ptr, st.Fp_old.ptr, st.Fp.ptr,
+                                                               status.ptr);
+  GOAL_CHECK_LAUNCH();
+  int h = 0;
+  GOAL_CUDA(cudaMemcpyAsync(&h, status.ptr, sizeof(int), cudaMemcpyDeviceToHost, disc->stream));
+  GOAL_CUDA(cudaStreamSynchronize(disc->stream));
+  GOAL_REQUIRE(h == 0, GOAL_ERR_RETURN_MAP, "J2: the exponential of the plastic increment did not converge");
+}
+
 void Mechanics::update_states() {
   const int E = disc->num_elems;
+  materialize_fp();
   GOAL_CUDA(cudaMemcpyAsync(st.Fp_old.ptr, st.Fp.ptr, sizeof(double) * 9 * E, cudaMemcpyDeviceToDevice, disc->stream));
   GOAL_CUDA(cudaMemcpyAsync(st.eqps_old.ptr, st.eqps.ptr, sizeof(double) * E, cudaMemcpyDeviceToDevice, disc->stream));
   refresh_cpinv();
@@ -982,6 +1016,8 @@ double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w,
   a.sigma = m.st.sigma.ptr;
   a.Fp = m.st.Fp.ptr;
   a.eqps = m.st.eqps.ptr;
+  a.Apend = m.st.Apend.ptr;
+  a.pend = m.st.pend.ptr;
   a.status = m.status.ptr;
   a.stab = m.stabilization ? 1 : 0;
   a.save = c.save_states;

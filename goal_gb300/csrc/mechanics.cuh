@@ -22,6 +22,12 @@ struct StatesDev {
   DevBuf<double> Fp, Fp_old;// 9 x E  plastic deformation gradient
   DevBuf<double> eqps, eqps_old;  // E
   DevBuf<double> Cpinv;     // 6 x E  Fp_old^{-1} Fp_old^{-T} (xx yy zz xy yz xz), refreshed with Fp_old
+  // Deferred Fp writes: a plastic point's state write stores the plastic
+  // increment A = dgam N (6 x E, xx yy zz xy yz xz) and sets pend; Fp =
+  // exp(A) Fp_old is formed when Fp is read or committed (materialize_fp),
+  // with the same arithmetic as an immediate write.
+  DevBuf<double> Apend;
+  DevBuf<int> pend;
 };
 
 struct Mechanics {
@@ -46,6 +52,7 @@ struct Mechanics {
   void init();
   void update_states();     // States::update (src/goal_states.cpp:130-141)
   void refresh_cpinv();
+  void materialize_fp();    // Fp = exp(A) Fp_old at points with a pending plastic write
 };
 
 // Linear objects of one discretization (LinearObj, src/goal_sol_info.hpp:12-16).

@@ -197,32 +197,148 @@ __device__ __forceinline__ void stage_edge(LayerSmem& sm, int w, int lane, const
   __syncwarp();
 }
 
+// ---------------------------------------------------------------- tensor cores
+// mma.sync m16n8k16, bfloat16 operands, FP32 accumulation. Fragment layout
+// (PTX ISA, m16n8k16 .bf16): g = lane / 4, q = lane % 4;
+//   A (16 x 16, row major): a0 = A[g][2q..2q+1], a1 = A[g+8][2q..], a2 = A[g][2q+8..], a3 = A[g+8][2q+8..]
+//   B (16 x 8, column major): b0 = B[2q..2q+1][g], b1 = B[2q+8..2q+9][g]
+//   C (16 x 8): c0, c1 = C[g][2q..2q+1], c2, c3 = C[g+8][2q..2q+1]
+// (each register holds two bfloat16, the lower column / row in the low half).
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+// two FP32 values as a bfloat16 pair split in two terms, x = hi + lo with
+// hi = rn(x), lo = rn(x - hi): the products with bfloat16 weights then carry
+// about 16 mantissa bits of the activations instead of 8
+__device__ __forceinline__ void split_bf16(float x0, float x1, unsigned& hi, unsigned& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+  hi = *reinterpret_cast<const unsigned*>(&h);
+  lo = *reinterpret_cast<const unsigned*>(&l);
+}
+
+constexpr int kIn = kME + kMH;       // 48 inputs of an edge message
+constexpr int kInStride = kIn + 4;   // staged row stride (floats)
+
+// One message-passing layer, forward: per node n (one warp),
+//   t_nm = We [e_nm; h_m] + be for its edges (m != n), agg = mean_m relu(t_nm),
+//   h_n' = h_n + relu(Wu [h_n; agg] + bu).
+// The edge messages are a (edges x 48) x (48 x 32) product: tiles of 16 edge
+// rows staged in shared memory go through the tensor cores (mma.sync, the
+// bfloat16 weights exact, the FP32 activations as two bfloat16 terms); the
+// node update (64 x 32 per node) stays on the CUDA cores. tbuf, ubuf and aggbuf
+// (training) keep t, the update's pre-activation and agg.
 __global__ void __launch_bounds__(256) k_layer_fwd(int N, const int* brow_ptr, const int* bcol, const double* A,
                                                     const double* sd, const int* deg, const unsigned short* wl,
                                                     const float* h_in, float* h_out, float* tbuf, float* ubuf,
                                                     float* aggbuf) {
   __shared__ LayerSmem sm;
+  __shared__ float sIn[kWarpsPerBlock][16][kInStride];
   load_layer(sm, wl);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  // B = We^T (48 x 32) fragments, kept in registers: k-step ks, n-tile nt
+  unsigned bfr[3][4][2];
+#pragma unroll
+  for (int ks = 0; ks < 3; ++ks)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const unsigned short* row = wl + MpnnLayout::We + (nt * 8 + g) * kIn + ks * 16 + 2 * q;
+      bfr[ks][nt][0] = (unsigned)row[0] | ((unsigned)row[1] << 16);
+      bfr[ks][nt][1] = (unsigned)row[8] | ((unsigned)row[9] << 16);
+    }
+  float bias[4][2];
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+    bias[nt][0] = sm.be[nt * 8 + 2 * q];
+    bias[nt][1] = sm.be[nt * 8 + 2 * q + 1];
+  }
+  float (*tile)[kInStride] = sIn[w];
   for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < N; n += (gridDim.x * blockDim.x) >> 5) {
-    float agg = 0.0f;
-    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
-      const int m = bcol[k];
-      if (m == n) continue;
-      stage_edge(sm, w, lane, A, k, sd, n, h_in, m);
-      float t = sm.be[lane];
-      for (int q = 0; q < kME + kMH; ++q) t += sm.We[lane][q] * sm.in[w][q];
-      if (tbuf) tbuf[32ll * k + lane] = t;
-      agg += fmaxf(t, 0.0f);
+    const int k0 = brow_ptr[n], k1 = brow_ptr[n + 1];
+    float aggp[4][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int kk = k0; kk < k1; kk += 16) {
+      // stage rows [e_nm (16); h_m (32)] of blocks kk .. kk+15 (zeros past the row's end)
+      for (int idx = lane; idx < 16 * kIn; idx += 32) {
+        const int r = idx / kIn, c = idx - r * kIn, k = kk + r;
+        float v = 0.0f;
+        if (k < k1) {
+          const int m = bcol[k];
+          v = c < kME ? (float)(sd[4ll * n + (c >> 2)] * A[16ll * k + c] * sd[4ll * m + (c & 3)])
+                      : h_in[32ll * m + (c - kME)];
+        }
+        tile[r][c] = v;
+      }
+      __syncwarp();
+      float acc[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        acc[nt][0] = acc[nt][2] = bias[nt][0];
+        acc[nt][1] = acc[nt][3] = bias[nt][1];
+      }
+#pragma unroll
+      for (int ks = 0; ks < 3; ++ks) {
+        const int c0 = ks * 16 + 2 * q;
+        unsigned ahi[4], alo[4];
+        split_bf16(tile[g][c0], tile[g][c0 + 1], ahi[0], alo[0]);
+        split_bf16(tile[g + 8][c0], tile[g + 8][c0 + 1], ahi[1], alo[1]);
+        split_bf16(tile[g][c0 + 8], tile[g][c0 + 9], ahi[2], alo[2]);
+        split_bf16(tile[g + 8][c0 + 8], tile[g + 8][c0 + 9], ahi[3], alo[3]);
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+          mma_bf16(acc[nt], ahi, bfr[ks][nt][0], bfr[ks][nt][1]);
+          mma_bf16(acc[nt], alo, bfr[ks][nt][0], bfr[ks][nt][1]);
+        }
+      }
+      // rows g and g + 8 of the tile: edges kk + g, kk + g + 8 (the diagonal block excluded)
+      const int ka = kk + g, kb = kk + g + 8;
+      const bool va = ka < k1 && bcol[ka] != n, vb = kb < k1 && bcol[kb] != n;
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        const int col = nt * 8 + 2 * q;
+        if (va) {
+          aggp[nt][0] += fmaxf(acc[nt][0], 0.0f);
+          aggp[nt][1] += fmaxf(acc[nt][1], 0.0f);
+          if (tbuf) *reinterpret_cast<float2*>(tbuf + 32ll * ka + col) = make_float2(acc[nt][0], acc[nt][1]);
+        }
+        if (vb) {
+          aggp[nt][0] += fmaxf(acc[nt][2], 0.0f);
+          aggp[nt][1] += fmaxf(acc[nt][3], 0.0f);
+          if (tbuf) *reinterpret_cast<float2*>(tbuf + 32ll * kb + col) = make_float2(acc[nt][2], acc[nt][3]);
+        }
+      }
       __syncwarp();
     }
-    agg /= (float)deg[n];
+    // sum over the eight row groups (lanes with the same q), in a fixed order
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        float v = aggp[nt][e];
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        v += __shfl_xor_sync(0xffffffffu, v, 8);
+        v += __shfl_xor_sync(0xffffffffu, v, 16);
+        aggp[nt][e] = v;
+      }
+    const float invdeg = 1.0f / (float)deg[n];
+    if (g == 0) {
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        sm.cat[w][kMH + nt * 8 + 2 * q] = aggp[nt][0] * invdeg;
+        sm.cat[w][kMH + nt * 8 + 2 * q + 1] = aggp[nt][1] * invdeg;
+      }
+    }
     const float hn = h_in[32ll * n + lane];
     sm.cat[w][lane] = hn;
-    sm.cat[w][kMH + lane] = agg;
     __syncwarp();
+    const float agg = sm.cat[w][kMH + lane];
     float u = sm.bu[lane];
-    for (int q = 0; q < 2 * kMH; ++q) u += sm.Wu[lane][q] * sm.cat[w][q];
+    for (int qq = 0; qq < 2 * kMH; ++qq) u += sm.Wu[lane][qq] * sm.cat[w][qq];
     if (ubuf) { ubuf[32ll * n + lane] = u; aggbuf[32ll * n + lane] = agg; }
     h_out[32ll * n + lane] = hn + fmaxf(u, 0.0f);
     __syncwarp();
@@ -350,6 +466,10 @@ __global__ void k_dW(int N, const double* g, const double* sd, const double* cha
     int n = i >> 4, r = (i >> 2) & 3, c = i & 3;
     if (kept(dmask, n, r) && kept(dmask, n, c)) dW[i] += coef * sd[4ll * n + r] * g[4ll * n + r] * chat[4ll * n + c];
   }
+}
+// loss += |S e|^2 / |S v|^2 of one probe (kept on the device; read once per step)
+__global__ void k_loss_acc(const double* scal, double* loss) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) loss[0] += scal[1] / scal[0];
 }
 __global__ void k_dC(int N, const double* dW, float* dC) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 16 * N; i += gridDim.x * blockDim.x) dC[i] = (float)dW[i];
@@ -567,6 +687,7 @@ void Mpnn::reserve(int N, int nnzb) {
     C.alloc(16ll * N);
     dC.alloc(16ll * N);
     dh.alloc(32ll * N);
+    dh_acc.alloc(32ll * N);
     dagg.alloc(32ll * N);
     s.alloc(N);
     sd.alloc(4ll * N);
@@ -633,10 +754,10 @@ double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const doubl
   net.dP.zero(st);
   const int vg = grid_for(n, 256);
   const int nb = std::min(grid_for(n, 256), 1024);
-  double* scal = net.red.ptr + 2 * 1024 + 2;  // [|S v|^2, |S e|^2]
+  double* scal = net.red.ptr + 2 * 1024 + 2;  // [|S v|^2, |S e|^2, loss]
   const int* bp = A.v.brow_ptr;
   const int* bc = A.v.bcol;
-  double loss = 0.0;
+  GOAL_CUDA(cudaMemsetAsync(scal + 2, 0, sizeof(double), st));
   for (int p = 0; p < num_probes; ++p) {
     if (probes_dev) {
       GOAL_CUDA(cudaMemcpyAsync(net.v.ptr, probes_dev + (size_t)p * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -680,10 +801,8 @@ double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const doubl
     k_dW<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.gT.ptr, net.sd.ptr, net.chat.ptr, net.dmask.ptr, scal,
                                                   net.dP.ptr);
     GOAL_CHECK_LAUNCH();
-    double hv[2];
-    GOAL_CUDA(cudaMemcpyAsync(hv, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    GOAL_CUDA(cudaStreamSynchronize(st));
-    loss += hv[1] / hv[0];
+    k_loss_acc<<<1, 32, 0, st>>>(scal, scal + 2);
+    GOAL_CHECK_LAUNCH();
   }
   k_dC<<<grid_for(16ll * N, 256), 256, 0, st>>>(N, net.dP.ptr, net.dC.ptr);
   GOAL_CHECK_LAUNCH();
@@ -694,8 +813,7 @@ double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const doubl
   k_decoder_bwd<<<kGridBlocks, 256, 0, st>>>(N, net.wbf.ptr, hbase + 32ll * N * kML, net.dC.ptr, net.dh.ptr,
                                               net.part.ptr, P);
   GOAL_CHECK_LAUNCH();
-  DevBuf<float> dh_acc;
-  dh_acc.alloc(32ll * N);
+  DevBuf<float>& dh_acc = net.dh_acc;
   for (int l = kML - 1; l >= 0; --l) {
     const int woff = MpnnLayout::L0 + l * MpnnLayout::layer;
     const unsigned short* wl = net.wbf.ptr + woff;
@@ -716,6 +834,8 @@ double mpnn_loss_grad(Mpnn& net, const BsrMatrix& A, int num_probes, const doubl
   GOAL_CHECK_LAUNCH();
   k_sum_parts<<<grid_for(P, 256), 256, 0, st>>>(P, kTotalWarps, net.part.ptr, net.grad.ptr);
   GOAL_CHECK_LAUNCH();
+  double loss = 0.0;
+  GOAL_CUDA(cudaMemcpyAsync(&loss, scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
   GOAL_CUDA(cudaStreamSynchronize(st));
   return loss;
 }

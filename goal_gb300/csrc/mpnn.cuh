@@ -51,7 +51,7 @@ struct Mpnn {
   DevBuf<unsigned short> wbf;           // bfloat16 copy used by the kernels
   long long adam_t = 0;
   // per-graph work buffers
-  DevBuf<float> x, h, t, u, agg, C, dC, dh, dagg, gbuf, grad, part;
+  DevBuf<float> x, h, t, u, agg, C, dC, dh, dh_acc, dagg, gbuf, grad, part;
   DevBuf<double> s, sd, Dinv, dP, y, r, gT, v, z, chat, red;
   DevBuf<int> tmap, deg, dmask;
   int cap_nodes = 0, cap_blocks = 0;

@@ -25,6 +25,9 @@ v_i = S^-1 w_i for even i and v_i = A D^-1 S^-1 w_i for odd i (weighted toward
 the high end of the spectrum, the part a node-local preconditioner acts on),
   L = sum_i |S (v_i - A P v_i)|^2 / |S v_i|^2.
 Weights are used rounded to bfloat16 (round to nearest even); all sums in float32.
+The edge messages' inputs [e_nm; h_m] enter the product with We as two
+bfloat16 terms, x = bf16(x) + bf16(x - bf16(x)) (the CUDA forward multiplies
+them on the tensor cores in that form).
 """
 from __future__ import annotations
 
@@ -72,6 +75,16 @@ def bf16(a):
     return r.astype(np.uint32).view(np.float32)
 
 
+def split_bf16(a):
+    """x as the sum of two bfloat16 terms, hi = bf16(x) + lo = bf16(x - hi),
+    in float32 (identity when ROUND_BF16 is off)."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if not ROUND_BF16:
+        return a
+    hi = bf16(a)
+    return (hi + bf16(a - hi)).astype(np.float32)
+
+
 def features(brow_ptr, bcol, diag, A):
     """A: (nnzb, 4, 4) float64 blocks. Returns x (N,20) f32, e (nnzb,16) f32,
     sd (N,4) f64 = |a_ii|^-1/2, Dinv (N,4,4), dirichlet (N,4) bool."""
@@ -115,7 +128,7 @@ def forward(params, brow_ptr, bcol, diag, x, e, keep=False):
     h = np.maximum(z0, 0).astype(np.float32)
     cache = {"z0": z0, "h": [h], "t": [], "agg": [], "u": []}
     for l in range(NL):
-        inp = np.concatenate([e[off], h[bcol[off]]], axis=1)
+        inp = split_bf16(np.concatenate([e[off], h[bcol[off]]], axis=1))
         t = inp @ p[f"We{l}"].T + p[f"be{l}"]
         msg = np.maximum(t, 0)
         agg = np.zeros((N, H), np.float32)
