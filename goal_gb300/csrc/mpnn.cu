@@ -538,37 +538,130 @@ __global__ void __launch_bounds__(256) k_layer_bwd_node(int N, const unsigned sh
   p[MpnnLayout::bu + lane] = gb;
 }
 
-// edge part: dt, dWe, dbe and g_k = (We^T dt)[16:] for every edge k = (n, m)
+// edge part: dt, dWe, dbe and g_k = (We^T dt)[16:] for every edge k = (n, m).
+// Per tile of 16 edge rows of a node (one warp), on the tensor cores:
+//   dWe (32 x 48) += dT^T (32 x 16) IN (16 x 48)   (both FP32 operands as two
+//                    bfloat16 terms; hi*hi + hi*lo + lo*hi, the lo*lo term
+//                    below FP32 rounding left out)
+//   G (16 x 32)    = dT (16 x 32) We_h (32 x 32)   (We_h = the h columns of We,
+//                    bfloat16 and exact; dT as two terms)
+// with dT[r][j] = da_n[j] where t_kj > 0 (0 on the diagonal block and past the
+// row's end). The dWe accumulators stay in registers for all of the warp's
+// nodes; dbe sums dT's columns on the CUDA cores.
 __global__ void __launch_bounds__(256) k_layer_bwd_edge(int N, const int* brow_ptr, const int* bcol, const double* A,
                                                          const double* sd, const unsigned short* wl, int woff,
                                                          const float* h_in, const float* tbuf, const float* dagg,
                                                          float* gbuf, float* part, int P) {
-  __shared__ LayerSmem sm;
-  load_layer(sm, wl);
+  __shared__ float sIn[kWarpsPerBlock][16][kInStride];
+  __shared__ float sdT[kWarpsPerBlock][16][kMH + 4];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane >> 2, q = lane & 3;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  float gW[kME + kMH];
-  for (int q = 0; q < kME + kMH; ++q) gW[q] = 0.0f;
+  // B = We_h (32 x 32), B[j][c] = We[j][16 + c]: k-step ks (j), n-tile nt (c)
+  unsigned bh[2][4][2];
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const unsigned short* col = wl + MpnnLayout::We + kME + nt * 8 + g;
+      const int j0 = ks * 16 + 2 * q;
+      bh[ks][nt][0] = (unsigned)col[j0 * kIn] | ((unsigned)col[(j0 + 1) * kIn] << 16);
+      bh[ks][nt][1] = (unsigned)col[(j0 + 8) * kIn] | ((unsigned)col[(j0 + 9) * kIn] << 16);
+    }
+  float gacc[2][6][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 6; ++nt) gacc[mt][nt][0] = gacc[mt][nt][1] = gacc[mt][nt][2] = gacc[mt][nt][3] = 0.0f;
   float gb = 0.0f;
+  float (*tile)[kInStride] = sIn[w];
+  float (*dT)[kMH + 4] = sdT[w];
   for (int n = gw; n < N; n += (gridDim.x * blockDim.x) >> 5) {
     const float da = dagg[32ll * n + lane];
-    for (int k = brow_ptr[n]; k < brow_ptr[n + 1]; ++k) {
-      const int m = bcol[k];
-      if (m == n) continue;
-      stage_edge(sm, w, lane, A, k, sd, n, h_in, m);
-      const float dt = (tbuf[32ll * k + lane] > 0.0f) ? da : 0.0f;
-      sm.d[w][lane] = dt;
+    const int k0 = brow_ptr[n], k1 = brow_ptr[n + 1];
+    for (int kk = k0; kk < k1; kk += 16) {
+      for (int idx = lane; idx < 16 * kIn; idx += 32) {
+        const int r = idx / kIn, c = idx - r * kIn, k = kk + r;
+        float v = 0.0f;
+        if (k < k1) {
+          const int m = bcol[k];
+          v = c < kME ? (float)(sd[4ll * n + (c >> 2)] * A[16ll * k + c] * sd[4ll * m + (c & 3)])
+                      : h_in[32ll * m + (c - kME)];
+        }
+        tile[r][c] = v;
+      }
+      // lane = output unit j: column j of dT
+      float colsum = 0.0f;
+#pragma unroll 4
+      for (int r = 0; r < 16; ++r) {
+        const int k = kk + r;
+        const bool live = k < k1 && bcol[k] != n;
+        const float dt = (live && tbuf[32ll * k + lane] > 0.0f) ? da : 0.0f;
+        dT[r][lane] = dt;
+        colsum += dt;
+      }
+      gb += colsum;
       __syncwarp();
-      for (int q = 0; q < kME + kMH; ++q) gW[q] += dt * sm.in[w][q];
-      gb += dt;
-      float g = 0.0f;
-      for (int j = 0; j < kMH; ++j) g += sm.We[j][kME + lane] * sm.d[w][j];
-      gbuf[32ll * k + lane] = g;
+      // dWe += dT^T IN: A = dT^T (rows j: m-tile mt; columns: the 16 edges), B = IN (edges x 48)
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        unsigned ahi[4], alo[4];
+        const int j = mt * 16 + g;
+        split_bf16(dT[2 * q][j], dT[2 * q + 1][j], ahi[0], alo[0]);
+        split_bf16(dT[2 * q][j + 8], dT[2 * q + 1][j + 8], ahi[1], alo[1]);
+        split_bf16(dT[2 * q + 8][j], dT[2 * q + 9][j], ahi[2], alo[2]);
+        split_bf16(dT[2 * q + 8][j + 8], dT[2 * q + 9][j + 8], ahi[3], alo[3]);
+#pragma unroll
+        for (int nt = 0; nt < 6; ++nt) {
+          const int c = nt * 8 + g;
+          unsigned bhi[2], blo[2];
+          split_bf16(tile[2 * q][c], tile[2 * q + 1][c], bhi[0], blo[0]);
+          split_bf16(tile[2 * q + 8][c], tile[2 * q + 9][c], bhi[1], blo[1]);
+          mma_bf16(gacc[mt][nt], ahi, bhi[0], bhi[1]);
+          mma_bf16(gacc[mt][nt], ahi, blo[0], blo[1]);
+          mma_bf16(gacc[mt][nt], alo, bhi[0], bhi[1]);
+        }
+      }
+      // G = dT We_h: A = dT (rows: edges; columns j), two k-steps of 16 j
+      float gk[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) gk[nt][0] = gk[nt][1] = gk[nt][2] = gk[nt][3] = 0.0f;
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks) {
+        const int c0 = ks * 16 + 2 * q;
+        unsigned ahi[4], alo[4];
+        split_bf16(dT[g][c0], dT[g][c0 + 1], ahi[0], alo[0]);
+        split_bf16(dT[g + 8][c0], dT[g + 8][c0 + 1], ahi[1], alo[1]);
+        split_bf16(dT[g][c0 + 8], dT[g][c0 + 9], ahi[2], alo[2]);
+        split_bf16(dT[g + 8][c0 + 8], dT[g + 8][c0 + 9], ahi[3], alo[3]);
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+          mma_bf16(gk[nt], ahi, bh[ks][nt][0], bh[ks][nt][1]);
+          mma_bf16(gk[nt], alo, bh[ks][nt][0], bh[ks][nt][1]);
+        }
+      }
+      const int ka = kk + g, kb = kk + g + 8;
+      const bool va = ka < k1 && bcol[ka] != n, vb = kb < k1 && bcol[kb] != n;
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        const int col = nt * 8 + 2 * q;
+        if (va) *reinterpret_cast<float2*>(gbuf + 32ll * ka + col) = make_float2(gk[nt][0], gk[nt][1]);
+        if (vb) *reinterpret_cast<float2*>(gbuf + 32ll * kb + col) = make_float2(gk[nt][2], gk[nt][3]);
+      }
       __syncwarp();
     }
   }
   float* p = part + (size_t)gw * P + woff;
-  for (int q = 0; q < kME + kMH; ++q) p[MpnnLayout::We + lane * (kME + kMH) + q] = gW[q];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 6; ++nt) {
+      const int j = mt * 16 + g, c = nt * 8 + 2 * q;
+      p[MpnnLayout::We + j * kIn + c] = gacc[mt][nt][0];
+      p[MpnnLayout::We + j * kIn + c + 1] = gacc[mt][nt][1];
+      p[MpnnLayout::We + (j + 8) * kIn + c] = gacc[mt][nt][2];
+      p[MpnnLayout::We + (j + 8) * kIn + c + 1] = gacc[mt][nt][3];
+    }
   p[MpnnLayout::be + lane] = gb;
 }
 
