@@ -47,6 +47,8 @@ def _args():
     ap.add_argument("--n", type=int, default=40, help="hexes per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--leg-budget", type=float, default=480.0,
+                    help="seconds after which no further solver leg is started")
     ap.add_argument("--adjoint-n", type=int, default=40, help="base mesh of the adjoint-solve leg (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=RAMP_STEPS, help="load steps of the adjoint leg's ramp")
     ap.add_argument("--precision-n", type=int, default=64,
@@ -63,6 +65,14 @@ def _args():
     ap.add_argument("--adaptive-growth", type=float, default=2.0, help="goal's \"target growth\" of the adaptive loop")
     ap.add_argument("--adaptive-steps", type=int, default=1, help="load steps of the adaptive loop")
     return ap.parse_args()
+
+
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Progress on stderr (the JSON line goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:8.1f}s] {msg}", file=sys.stderr, flush=True)
 
 
 # ------------------------------------------------------------------ workload
@@ -304,7 +314,7 @@ ETA_BAR = 1e-8      # |eta - eta_ref| / |eta_ref| that every arm must hold
 
 
 def _j2_ramp(api, n, steps, seed=1, max_newton=60, precision=None, lin_tol=1e-10, qoi=False, fp_reset=True,
-             line_search=8, cutbacks=4, lin_max_iters=3000):
+             line_search=8, cutbacks=4, lin_max_iters=3000, jitter=None):
     """``steps`` J2 load steps of the stretched cube (u = 0 on x=0, u_x =
     LOAD_INC t on x=1 at t = 1, 2, ...), the states updated between steps, on a
     Kuhn cube with jittered interior nodes (no grid symmetry), with goal's
@@ -319,7 +329,8 @@ def _j2_ramp(api, n, steps, seed=1, max_newton=60, precision=None, lin_tol=1e-10
     (the solution is restored; with fp_reset every state the failed solve wrote
     is rewritten by the next one). line_search = cutbacks = 0 is goal's Newton."""
     from goal_gb300.mesh import kuhn_cube
-    mesh = kuhn_cube(n, jitter=JITTER, seed=seed)
+    jit = JITTER if jitter is None else jitter
+    mesh = kuhn_cube(n, jitter=jit, seed=seed) if jit > 0 else kuhn_cube(n)
     d = api.Disc(mesh)
     m = api.Mechanics(d, api.J2, [[MAT["E"], MAT["nu"], MAT["K"], MAT["Y"], MAT["c0"]]], fp_reset=fp_reset)
     if line_search:
@@ -340,9 +351,13 @@ def _j2_ramp(api, n, steps, seed=1, max_newton=60, precision=None, lin_tol=1e-10
                 pending_update = False
             U0 = m.get_solution() if cutbacks else None
             try:
+                tn = time.perf_counter()
                 newton = api.primal_solve(m, s, bcs, t_now, t_old, max_newton, 1e-8, prm)
+                log(f"ramp n={n} t={t_now:g}: {newton['iters']} Newton iterations, {newton['linear_iters']} linear, "
+                    f"{newton['backtracks']} backtracks, {time.perf_counter() - tn:.1f}s")
             except api.GoalError as e:
                 its += len(getattr(e, "stats", {}).get("norms") or [])
+                log(f"ramp n={n} t={t_now:g}: Newton failed ({time.perf_counter() - tn:.1f}s)")
                 if depth >= cutbacks:
                     e.step = k
                     raise
@@ -389,8 +404,8 @@ def adjoint_arms(api, plain=True, learned_fp64=True):
     the nested FGMRES(30) solves with 60 inner iterations in FP64, FP32 and
     binary16 storage (FP64 outer residual and update), and the learned
     correction inside the FP32 and binary16 nested solves."""
-    nest = dict(krylov_size=30, tolerance=ADJ_TOL, max_iters=3000, inner_iters=INNER_ITERS)
-    lrn = dict(precond=api.PRECOND_LEARNED, learned_cap=1500)
+    nest = dict(krylov_size=30, tolerance=ADJ_TOL, max_iters=1000, inner_iters=INNER_ITERS)
+    lrn = dict(precond=api.PRECOND_LEARNED, learned_cap=500)
     arms = {}
     if plain:
         arms["plain_fp64"] = api.solve_params(krylov_size=100, tolerance=ADJ_TOL, max_iters=45000)
@@ -469,9 +484,12 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
         r = na.run(api.QOI_KS_VM, 20.0, t_now, t_old, prm)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
-        return _solve_record(r)
+        rec = _solve_record(r)
+        log(f"adjoint n={n} {name}: {rec['seconds']:.2f}s, {rec['iters']} iterations, converged {rec['converged']}, "
+            f"eta {rec['eta']:.12e}")
+        return rec
 
-    nest = dict(krylov_size=30, max_iters=3000, inner_iters=INNER_ITERS)
+    nest = dict(krylov_size=30, max_iters=1000, inner_iters=INNER_ITERS)
     ref = run("reference", api.solve_params(precision=api.NESTED_F64, tolerance=REF_TOL, **nest))
     chk = run("reference_check", api.solve_params(precision=api.MIXED, tolerance=REF_TOL,
                                                   precond=api.PRECOND_LEARNED, learned_cap=3000, **nest))
@@ -910,33 +928,7 @@ def main():
                      "binding_roof": "fp64", "fp64": fp64},
         "clocks": clk,
     }
-    if a.learned_eval > 0:
-        try:
-            if a.learned_scale == "full":
-                line["learned_eval"] = learned_eval_leg(api, a.learned_eval, train_problems=34,
-                                                        train_target=(100000, 400000), eval_target=(100000, 400000),
-                                                        epochs=10, eval_steps=5)
-            else:
-                line["learned_eval"] = learned_eval_leg(api, a.learned_eval)
-        except Exception as exc:
-            line["learned_eval"] = {"error": str(exc)[:300]}
-    if a.adaptive_cycles > 0:
-        try:
-            line["adaptive_loop"] = adaptive_leg(api, a.adaptive_cycles, a.adaptive_start, growth=a.adaptive_growth,
-                                                 steps=a.adaptive_steps)
-        except Exception as exc:
-            line["adaptive_loop"] = {"error": str(exc)[:300]}
-    if a.adjoint_n > 0:
-        try:
-            line["adjoint_solve"] = adjoint_leg(a.adjoint_n, api, steps=a.adjoint_steps, qoi_check=False)
-        except Exception as exc:  # the assembly line stands on its own
-            line["adjoint_solve"] = {"error": str(exc)[:300]}
-    if a.precision_n > 0:
-        try:
-            line["precision_64"] = adjoint_leg(a.precision_n, api, steps=a.precision_steps, learned_fp64=False,
-                                               goal_attempts=False)
-        except Exception as exc:
-            line["precision_64"] = {"error": str(exc)[:300]}
+    log(f"assembly: {value:.4g} elem/s")
     if not a.no_cpu_baseline:
         rate, ne = cpu_assembly_rate(mesh, u, p, Fp_old, eqps_old, a.cpu_seconds, False)
         line["cpu_baseline"] = {"value": rate, "unit": "elem/s", "cores": 1, "kind": "port",
@@ -951,6 +943,38 @@ def main():
                                                     f"threads"}
         except Exception as exc:
             line["cpu_baseline_tuned"] = {"error": str(exc)[:200]}
+        log(f"CPU baselines: {line['cpu_baseline']['value']:.4g} elem/s (1 thread), tuned "
+            f"{line['cpu_baseline_tuned'].get('value', 0.0):.4g} elem/s")
+
+    # the solver legs, most important first, within a time budget (each leg's
+    # result also goes to stderr as soon as it is there)
+    legs = []
+    if a.adjoint_n > 0:
+        legs.append(("adjoint_solve", lambda: adjoint_leg(a.adjoint_n, api, steps=a.adjoint_steps, qoi_check=False)))
+    if a.adaptive_cycles > 0:
+        legs.append(("adaptive_loop", lambda: adaptive_leg(api, a.adaptive_cycles, a.adaptive_start,
+                                                           growth=a.adaptive_growth, steps=a.adaptive_steps)))
+    if a.learned_eval > 0:
+        if a.learned_scale == "full":
+            legs.append(("learned_eval", lambda: learned_eval_leg(api, a.learned_eval, train_problems=34,
+                                                                  train_target=(100000, 400000),
+                                                                  eval_target=(100000, 400000), epochs=10,
+                                                                  eval_steps=5)))
+        else:
+            legs.append(("learned_eval", lambda: learned_eval_leg(api, a.learned_eval)))
+    if a.precision_n > 0:
+        legs.append(("precision_64", lambda: adjoint_leg(a.precision_n, api, steps=a.precision_steps,
+                                                         learned_fp64=False, goal_attempts=False)))
+    t_legs = time.perf_counter()
+    for name, fn in legs:
+        if time.perf_counter() - t_legs > a.leg_budget:
+            line[name] = {"skipped": f"time budget of {a.leg_budget:g} s for the solver legs spent"}
+            continue
+        try:
+            line[name] = fn()
+        except Exception as exc:  # the assembly line stands on its own
+            line[name] = {"error": str(exc)[:300]}
+        log(f"{name}: " + json.dumps(line[name], default=str)[:4000])
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
