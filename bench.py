@@ -426,7 +426,8 @@ def _solve_record(r):
             "rel_res": r["solve"]["rel_res"], "eta": r["eta"], "bound": r["bound"]}
 
 
-def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_check=True, goal_attempts=True):
+def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_check=True, goal_attempts=True,
+                ramp=None):
     """Adjoint solve on the nested (uniformly refined) mesh after the J2 load
     ramp of the stretched cube (u_x = LOAD_INC t on x=1, t = 1..steps; u=0 on
     x=0): dRdu^T z = dM/du with the KS von Mises functional (rho = 20), the
@@ -443,22 +444,29 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
     reports the per-step QoI deviation of the production ramp (mixed linear
     solves to 1e-10). ``goal_attempts`` first runs the ramp with goal's own
     Newton (full steps, max 15 iterations) with goal's J2 state write and with
-    the Fp_old reset, and reports the step where each stops converging."""
+    the Fp_old reset, and reports the step where each stops converging.
+    ``ramp``: the globalization of the load ramp (_j2_ramp's jitter,
+    line_search, cutbacks, max_newton)."""
     import torch
-    out = {"mesh": f"kuhn cube {n}^3 x 6 tets, interior nodes jittered by {JITTER} h, refined once",
+    ramp = dict(ramp or {})
+    jit = ramp.get("jitter", JITTER)
+    out = {"mesh": f"kuhn cube {n}^3 x 6 tets" + (f", interior nodes jittered by {jit} h" if jit > 0 else "") +
+                   ", refined once",
            "load": f"u_x = {LOAD_INC} t on x=1, {steps} steps (u_x = {LOAD_INC * steps:g})",
-           "newton": "Fp_old reset at elastic points, line search (8 halvings), up to 4 halvings of a failed "
-                     "load increment, 60 iterations, |R| < 1e-8"}
+           "newton": f"Fp_old reset at elastic points, line search {ramp.get('line_search', 8)} halvings, up to "
+                     f"{ramp.get('cutbacks', 4)} halvings of a failed load increment, "
+                     f"{ramp.get('max_newton', 60)} iterations per solve, |R| < 1e-8"}
     if goal_attempts:
         for key, reset in (("goal_newton", False), ("goal_newton_fp_reset", True)):
             try:
-                _j2_ramp(api, n, steps, fp_reset=reset, line_search=0, cutbacks=0, max_newton=15, lin_max_iters=300)
+                _j2_ramp(api, n, steps, fp_reset=reset, line_search=0, cutbacks=0, max_newton=15, lin_max_iters=300,
+                         jitter=jit)
                 out[key] = {"failed_at_step": None}
             except api.GoalError as e:
                 nrm = getattr(e, "stats", {}).get("norms") or []
                 out[key] = {"failed_at_step": getattr(e, "step", None), "newton_norms": [float(x) for x in nrm]}
     t0 = time.perf_counter()
-    mesh, d, m, s, bcs, dbcs, newton = _j2_ramp(api, n, steps, qoi=True)
+    mesh, d, m, s, bcs, dbcs, newton = _j2_ramp(api, n, steps, qoi=True, **ramp)
     t_primal = time.perf_counter() - t0
     out.update({"base_elements": mesh.num_elems, "newton_iters": newton["iters"], "load_substeps": newton["substeps"],
                 "primal_seconds": t_primal,
@@ -466,7 +474,7 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
                 "reference_tolerance": REF_TOL})
     if qoi_check:
         t1 = time.perf_counter()
-        ref_p = _j2_ramp(api, n, steps, precision=api.NESTED_F64, lin_tol=1e-12, qoi=True)
+        ref_p = _j2_ramp(api, n, steps, precision=api.NESTED_F64, lin_tol=1e-12, qoi=True, **ramp)
         Jr = ref_p[-1]["J"]
         out["qoi_reference"] = {"linear": "nested FGMRES, FP64 inner and outer, to 1e-12",
                                 "newton_iters": ref_p[-1]["iters"], "seconds": time.perf_counter() - t1,
@@ -842,22 +850,26 @@ def main():
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     launches0 = L.goal_launch_count()
-    L.goal_assembly_timing(1)
     ev0.record(stream)
     for _ in range(a.steps):
         step()
     ev1.record(stream)
     ev1.synchronize()
-    L.goal_assembly_timing(0)
     launches = L.goal_launch_count() - launches0
+    barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / a.steps, world, "cuda")
+    # the two phases' device times (CUDA events around them inside the library),
+    # in a separate loop so that the events do not weigh on the timed steps
     import ctypes
+    L.goal_assembly_timing(1)
+    for _ in range(min(a.steps, 50)):
+        step()
+    L.goal_assembly_timing(0)
     phase_ms = (ctypes.c_double * 2)()
     phase_n = ctypes.c_longlong()
     L.goal_assembly_timing_read(phase_ms, ctypes.byref(phase_n))
     elem_ms = phase_ms[0] / max(1, phase_n.value)
     gather_ms = phase_ms[1] / max(1, phase_n.value)
-    barrier()
-    ms = max_over_ranks(ev0.elapsed_time(ev1) / a.steps, world, "cuda")
 
     # end to end through the public API: pinned host U in, host R out, every step
     Uh = torch.from_numpy(U.ravel().copy()).pin_memory()
@@ -950,7 +962,11 @@ def main():
     # result also goes to stderr as soon as it is there)
     legs = []
     if a.adjoint_n > 0:
-        legs.append(("adjoint_solve", lambda: adjoint_leg(a.adjoint_n, api, steps=a.adjoint_steps, qoi_check=False)))
+        # the literal configuration's mesh (no jitter); goal's full Newton steps
+        # with load-increment cutbacks (backtracking stalls on this cube)
+        legs.append(("adjoint_solve", lambda: adjoint_leg(a.adjoint_n, api, steps=a.adjoint_steps, qoi_check=False,
+                                                          ramp=dict(jitter=0.0, line_search=0, cutbacks=6,
+                                                                    max_newton=15))))
     if a.adaptive_cycles > 0:
         legs.append(("adaptive_loop", lambda: adaptive_leg(api, a.adaptive_cycles, a.adaptive_start,
                                                            growth=a.adaptive_growth, steps=a.adaptive_steps)))
@@ -963,8 +979,11 @@ def main():
         else:
             legs.append(("learned_eval", lambda: learned_eval_leg(api, a.learned_eval)))
     if a.precision_n > 0:
+        # jittered 64^3 cube: full Newton fails at the first step there, backtracking converges every step
         legs.append(("precision_64", lambda: adjoint_leg(a.precision_n, api, steps=a.precision_steps,
-                                                         learned_fp64=False, goal_attempts=False)))
+                                                         learned_fp64=False, goal_attempts=False,
+                                                         ramp=dict(jitter=JITTER, line_search=8, cutbacks=6,
+                                                                   max_newton=30))))
     t_legs = time.perf_counter()
     for name, fn in legs:
         if time.perf_counter() - t_legs > a.leg_budget:
