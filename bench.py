@@ -51,8 +51,8 @@ def _args():
                     help="seconds after which no further solver leg is started")
     ap.add_argument("--adjoint-n", type=int, default=40, help="base mesh of the adjoint-solve leg (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=RAMP_STEPS, help="load steps of the adjoint leg's ramp")
-    ap.add_argument("--precision-n", type=int, default=64,
-                    help="base mesh of the precision leg (FP32-inner vs FP64 adjoint at 64^3; 0: skip)")
+    ap.add_argument("--precision-n", type=int, default=0,
+                    help="base mesh of the precision leg (64: the 64^3 cube of the precision configuration; 0: skip)")
     ap.add_argument("--precision-steps", type=int, default=10, help="load steps of the precision leg's ramp")
     ap.add_argument("--learned-eval", type=int, default=20,
                     help="held-out seeds of the learned-preconditioner study (0: skip)")
@@ -309,12 +309,12 @@ RAMP_STEPS = 10     # u_x = 0.02 at the last step
 INNER_ITERS = 60
 JITTER = 0.2
 ADJ_TOL = 1e-10     # the metric's relative residual
-REF_TOL = 1e-13     # the FP64 reference adjoint solve
+REF_TOL = 1e-12     # the FP64 reference adjoint solve
 ETA_BAR = 1e-8      # |eta - eta_ref| / |eta_ref| that every arm must hold
 
 
-def _j2_ramp(api, n, steps, seed=1, max_newton=60, precision=None, lin_tol=1e-10, qoi=False, fp_reset=True,
-             line_search=8, cutbacks=4, lin_max_iters=3000, jitter=None):
+def _j2_ramp(api, n, steps, seed=1, max_newton=12, precision=None, lin_tol=1e-10, qoi=False, fp_reset=True,
+             line_search=0, cutbacks=6, lin_max_iters=400, jitter=None):
     """``steps`` J2 load steps of the stretched cube (u = 0 on x=0, u_x =
     LOAD_INC t on x=1 at t = 1, 2, ...), the states updated between steps, on a
     Kuhn cube with jittered interior nodes (no grid symmetry), with goal's
@@ -327,7 +327,9 @@ def _j2_ramp(api, n, steps, seed=1, max_newton=60, precision=None, lin_tol=1e-10
     failure): ``line_search`` step halvings on ||R|| per Newton iteration, and
     up to ``cutbacks`` halvings of a load increment whose Newton solve fails
     (the solution is restored; with fp_reset every state the failed solve wrote
-    is rewritten by the next one). line_search = cutbacks = 0 is goal's Newton."""
+    is rewritten by the next one). The increment of the last success is tried
+    first and doubled after four successes in a row. line_search = cutbacks = 0
+    is goal's Newton."""
     from goal_gb300.mesh import kuhn_cube
     jit = JITTER if jitter is None else jitter
     mesh = kuhn_cube(n, jitter=jit, seed=seed) if jit > 0 else kuhn_cube(n)
@@ -342,8 +344,9 @@ def _j2_ramp(api, n, steps, seed=1, max_newton=60, precision=None, lin_tol=1e-10
     prm = api.solve_params(tolerance=lin_tol, precision=prec, inner_iters=30, krylov_size=30, max_iters=lin_max_iters)
     iters, Js, subs = [], [], []
     t_old, pending_update = 0.0, False
+    depth, streak = 0, 0
     for k in range(1, steps + 1):
-        its, nsub, depth = 0, 0, 0
+        its, nsub = 0, 0
         while t_old < k - 1e-12:
             t_now = min(float(k), t_old + 2.0 ** -depth)
             if pending_update:
@@ -363,11 +366,16 @@ def _j2_ramp(api, n, steps, seed=1, max_newton=60, precision=None, lin_tol=1e-10
                     raise
                 m.set_solution(U0)
                 depth += 1
+                streak = 0
                 continue
             its += newton["iters"]
             nsub += 1
             t_old = t_now
             pending_update = True
+            streak += 1
+            if streak >= 4 and depth > 0:
+                depth -= 1
+                streak = 0
         iters.append(its)
         subs.append(nsub)
         if qoi:
@@ -474,9 +482,9 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
                 "reference_tolerance": REF_TOL})
     if qoi_check:
         t1 = time.perf_counter()
-        ref_p = _j2_ramp(api, n, steps, precision=api.NESTED_F64, lin_tol=1e-12, qoi=True, **ramp)
+        ref_p = _j2_ramp(api, n, steps, precision=api.NESTED_F64, qoi=True, **ramp)
         Jr = ref_p[-1]["J"]
-        out["qoi_reference"] = {"linear": "nested FGMRES, FP64 inner and outer, to 1e-12",
+        out["qoi_reference"] = {"linear": "nested FGMRES, FP64 inner and outer, to the same 1e-10",
                                 "newton_iters": ref_p[-1]["iters"], "seconds": time.perf_counter() - t1,
                                 "J_rel_dev_max": max(abs(a - b) / abs(b) for a, b in zip(newton["J"], Jr)),
                                 "J_rel_dev_last": abs(newton["J"][-1] - Jr[-1]) / abs(Jr[-1])}
@@ -965,8 +973,7 @@ def main():
         # the literal configuration's mesh (no jitter); goal's full Newton steps
         # with load-increment cutbacks (backtracking stalls on this cube)
         legs.append(("adjoint_solve", lambda: adjoint_leg(a.adjoint_n, api, steps=a.adjoint_steps, qoi_check=False,
-                                                          ramp=dict(jitter=0.0, line_search=0, cutbacks=6,
-                                                                    max_newton=15))))
+                                                          ramp=dict(jitter=0.0))))
     if a.adaptive_cycles > 0:
         legs.append(("adaptive_loop", lambda: adaptive_leg(api, a.adaptive_cycles, a.adaptive_start,
                                                            growth=a.adaptive_growth, steps=a.adaptive_steps)))
@@ -982,8 +989,8 @@ def main():
         # jittered 64^3 cube: full Newton fails at the first step there, backtracking converges every step
         legs.append(("precision_64", lambda: adjoint_leg(a.precision_n, api, steps=a.precision_steps,
                                                          learned_fp64=False, goal_attempts=False,
-                                                         ramp=dict(jitter=JITTER, line_search=8, cutbacks=6,
-                                                                   max_newton=30))))
+                                                         ramp=dict(jitter=JITTER, line_search=8, max_newton=30,
+                                                                   lin_max_iters=3000))))
     t_legs = time.perf_counter()
     for name, fn in legs:
         if time.perf_counter() - t_legs > a.leg_budget:

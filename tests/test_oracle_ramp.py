@@ -8,15 +8,19 @@ With the configuration's increment of 0.002 per load step (u_x = 0.02 in 10
 steps) the third step diverges: the residual grows every iteration until the
 return map sees non-finite strains. With 0.0005 per step every step converges
 in 7 iterations or fewer on this mesh (a full run to u_x = 0.02, 40 steps,
-converges throughout; on the 40^3 cube even 0.0005 stops converging at
-u_x = 0.0035).
+converges throughout).
 
-The cause is goal's J2 state write (src/goal_J2.cpp:97-136): Fp is written
-only at points that yield, so at a point that is plastic in an early Newton
-iterate and elastic at convergence the early iterate's Fp survives, and
-States::update commits it as Fp_old. With the Fp_old reset option (Fp =
-Fp_old at elastic points; off by default, goal's behaviour otherwise) the
-configuration's own ramp converges in 7 or 8 iterations per step."""
+On this mesh the cause is goal's J2 state write (src/goal_J2.cpp:97-136): Fp
+is written only at points that yield, so at a point that is plastic in an
+early Newton iterate and elastic at convergence the early iterate's Fp
+survives, and States::update commits it as Fp_old. With the Fp_old reset
+option (Fp = Fp_old at elastic points; off by default, goal's behaviour
+otherwise) the configuration's own ramp converges in 7 or 8 iterations per
+step. Finer meshes need more: the same full Newton with the reset reproduces
+the oracle's iterates on the 16^3 cube and converges there, but stops at the
+second step on the 24^3 cube and at the first on the 40^3 cube, where only
+halving the failed load increments (a driver-level cutback, not in goal)
+carries the ramp to u_x = 0.02."""
 import numpy as np
 import pytest
 
