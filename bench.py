@@ -616,12 +616,14 @@ def learned_eval_leg(api, held_out, train_problems=8, train_target=20000, eval_t
             continue
         keep.append(prob)
         elems.append(prob[0].num_elems)
+        log(f"learned study: training problem {seed}: {prob[0].num_elems} elements, {len(systems)} systems")
         train += [sk for _, sk in systems]
         keep.append(systems)
     net = api.Learned(seed=0)
     t1 = time.perf_counter()
     losses = net.train(train, epochs=epochs, lr=2e-3, num_probes=8)
     t_train = time.perf_counter() - t1
+    log(f"learned study: trained on {len(train)} systems, {epochs} epochs in {t_train:.1f}s")
     out = {"train": {"problems": train_problems - failed, "systems": len(train), "elements_each": train_target,
                      "elements_min": min(elems) if elems else 0, "elements_max": max(elems) if elems else 0,
                      "epochs": epochs, "seconds_generate": t1 - t0, "seconds_train": t_train,
@@ -644,6 +646,8 @@ def learned_eval_leg(api, held_out, train_problems=8, train_target=20000, eval_t
             net.attach(sk)
             _, lrn = api.solve(sk, b, params=api.solve_params(precond=api.PRECOND_LEARNED, learned_cap=750, **mix))
             rows[kind].append((plain, lrn))
+            log(f"learned study: seed {seed} {kind}: plain {plain['iters']} its {plain['seconds']:.3f}s, "
+                f"learned {lrn['iters']} its {lrn['seconds']:.3f}s")
     out["newton_failures"] = eval_failed
     if eval_elems:
         out["elements_min"], out["elements_max"] = min(eval_elems), max(eval_elems)
@@ -791,6 +795,7 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
                           "Fp_old": m.get_state(api.FP_OLD), "eqps": m.get_state(api.EQPS),
                           "eqps_old": m.get_state(api.EQPS_OLD)}
             out.append(rec)
+            log("adaptive cycle: " + json.dumps({k: v for k, v in rec.items() if not isinstance(v, dict)}))
             del m, s, bcs, d
     return out
 
