@@ -941,6 +941,11 @@ def main():
                 "flop_per_element": pr["fp64_flop_per_element"],
                 "peak_source": "measured in this run: independent DFMA chains on every SM (goal_measure_fp64_peak)",
                 "nominal_peak": FP64_PEAK_TFLOPS}
+        # the FP64 pipe issues one instruction (DFMA, DMUL or DADD) per slot:
+        # the issue rate against the probe's DFMA rate (peak / 2 FLOP)
+        instr = sum(pr["fp64_instructions_per_element"].values()) * E
+        fp64["instructions_per_element"] = sum(pr["fp64_instructions_per_element"].values())
+        fp64["issue_frac"] = instr / (elem_ms * 1e-3) / (fp64_peak * 1e12 / 2.0)
     line = {
         "metric": METRIC, "value": value, "unit": "elem/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",

@@ -998,9 +998,18 @@ void set_element_buffer_limit(long long bytes) { g_ebuf_limit = bytes < 0 ? 0 : 
 
 long long element_buffer_limit() {
   if (g_ebuf_limit > 0) return g_ebuf_limit;
-  size_t free_b = 0, total_b = 0;
-  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || total_b == 0) return 8ll << 30;
-  return (long long)(total_b / 4);
+  // a quarter of the device's memory, looked up once per device (the query is
+  // too slow to repeat in every assembly)
+  constexpr int kDevs = 64;
+  static long long total[kDevs] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevs) return 8ll << 30;
+  if (total[dev] == 0) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || total_b == 0) return 8ll << 30;
+    total[dev] = (long long)total_b;
+  }
+  return total[dev] / 4;
 }
 
 double assemble(Mechanics& m, SolInfo* s, const Chain& c, const ErrorWeights* w, cudaStream_t st) {
