@@ -448,9 +448,9 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
     its eta and bound deviation from the reference. The learned + binary16
     arm is solved again to the tolerance that holds eta within ETA_BAR
     (1e-11, else 1e-12), the time that counts against plain FP64.
-    ``qoi_check`` repeats the load ramp with FP64 linear solves to REF_TOL and
-    reports the per-step QoI deviation of the production ramp (mixed linear
-    solves to 1e-10). ``goal_attempts`` first runs the ramp with goal's own
+    ``qoi_check`` repeats the load ramp with FP64 nested linear solves (FP64
+    inner iterations and storage) to the same 1e-10 and reports the per-step
+    QoI deviation of the production ramp (binary16-inner linear solves). ``goal_attempts`` first runs the ramp with goal's own
     Newton (full steps, max 15 iterations) with goal's J2 state write and with
     the Fp_old reset, and reports the step where each stops converging.
     ``ramp``: the globalization of the load ramp (_j2_ramp's jitter,
@@ -598,7 +598,8 @@ def learned_eval_leg(api, held_out, train_problems=8, train_target=20000, eval_t
     problems (5 load steps each: every Newton Jacobian plus the adjoint one),
     then solve the last Newton Jacobian and the adjoint system of ``held_out``
     other seeds (``eval_steps`` load steps), right-hand side avg disp's dM/du,
-    to 1e-10 with FP32-inner / FP64-outer FGMRES, once with plain block-Jacobi
+    to 1e-10 with nested FGMRES (inner iterations on a binary16-stored copy
+    with FP32 arithmetic, FP64 outer), once with plain block-Jacobi
     and once with the network: outer iterations, seconds and how often the cap
     (750 outer iterations) sent the solve back to plain block-Jacobi. (Plain
     FP64 block-Jacobi FGMRES(100) needs more than 20,000 iterations on most of
@@ -686,12 +687,19 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
     target_elems * growth^(cycle - 1) (target_elems = start * growth, so the
     first adaptation keeps the element count) and the adaptation (coarsening,
     then refinement) with the fields carried over; the states are updated
-    after a step's cycles. The nested adjoint is solved to 1e-10 with FP32-inner
-    / FP64-outer FGMRES, with plain block-Jacobi and with the network trained
+    after a step's cycles. The nested adjoint is solved to 1e-10 with nested
+    FGMRES (binary16-stored inner iterations in FP32 arithmetic, FP64 outer),
+    with plain block-Jacobi and with the network trained
     on the cycle's Newton Jacobian, against an FP64 reference to REF_TOL (FP64
     nested FGMRES; learned + binary16 FGMRES beyond fp64_reference_max_dofs,
     where the FP64 inner basis would not fit beside the rest), and the
-    learned solve again at the loosest tolerance that holds eta within ETA_BAR."""
+    learned solve again at the loosest tolerance that holds eta within ETA_BAR.
+
+    goal aborts the run when a Newton solve fails (src/goal_primal.cpp:131-136).
+    Here a failed solve is retried once from the same start (the transferred
+    solution and states) with backtracking on ||R|| (8 halvings, 30
+    iterations), a globalization goal does not have, and the record says so; a
+    second failure ends the leg with the cycles done so far."""
     import torch
     from goal_gb300 import adapt
     from goal_gb300.mesh import graded_block
@@ -710,16 +718,37 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
         t_now, t_old = float(step), float(step - 1)
         for cycle in range(cycles + 1):
             d = api.Disc(mesh)
-            m = api.Mechanics(d, api.J2, mats)
-            if U is not None:
-                m.set_solution(U.ravel())
-                for k, v in states.items():
-                    m.set_state({"sigma": api.SIGMA, "Fp": api.FP, "Fp_old": api.FP_OLD, "eqps": api.EQPS,
-                                 "eqps_old": api.EQPS_OLD}[k], v)
+
+            def start_mechanics():
+                mech = api.Mechanics(d, api.J2, mats)
+                if U is not None:
+                    mech.set_solution(U.ravel())
+                    for k, v in states.items():
+                        mech.set_state({"sigma": api.SIGMA, "Fp": api.FP, "Fp_old": api.FP_OLD, "eqps": api.EQPS,
+                                        "eqps_old": api.EQPS_OLD}[k], v)
+                return mech
+
+            m = start_mechanics()
             s = api.SolInfo(d)
             bcs = api.Bcs(d, dbcs, [])
             t0 = time.perf_counter()
-            newton = api.primal_solve(m, s, bcs, t_now, t_old, 15, 1e-8, newton_prm)
+            retry = None
+            try:
+                newton = api.primal_solve(m, s, bcs, t_now, t_old, 15, 1e-8, newton_prm)
+            except api.GoalError as exc:
+                retry = {"goal_newton": str(exc)[:160], "retry": "backtracking on ||R||, 8 halvings, 30 iterations"}
+                log(f"adaptive cycle {cycle}: {exc}; retrying with backtracking")
+                m = start_mechanics()
+                m.set_line_search(8)
+                try:
+                    newton = api.primal_solve(m, s, bcs, t_now, t_old, 30, 1e-8, newton_prm)
+                except api.GoalError as exc2:
+                    out.append({"step": step, "cycle": cycle, "elements": mesh.num_elems, "dofs": d.num_dofs,
+                                "newton_failed": dict(retry, retry_error=str(exc2)[:160])})
+                    log("adaptive cycle: " + json.dumps(out[-1]))
+                    return out
+                retry["retry_iters"] = newton["iters"]
+                retry["retry_backtracks"] = newton["backtracks"]
             t_newton = time.perf_counter() - t0
             J = api.assemble(m, None, api.NONE, jacobian=False, save_states=False, qoi=api.QOI_KS_VM, rho=20.0)
             stream = torch.cuda.ExternalStream(d.stream())
@@ -734,6 +763,7 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
             alg = algorithmic_bytes(d.num_nodes, d.num_elems, d.nnz)
             rec = {"step": step, "cycle": cycle, "elements": mesh.num_elems, "dofs": d.num_dofs,
                    "newton_iters": newton["iters"], "newton_seconds": t_newton, "J": J,
+                   **({"newton_retry": retry} if retry else {}),
                    "assembly_elem_per_s": mesh.num_elems / (ms * 1e-3), "assembly_ms": ms,
                    "assembly_hbm_gbs": alg / (ms * 1e-3) / 1e9}
             if cycle < cycles:
@@ -770,7 +800,9 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
                            adjoint_learned_mixed={"seconds": r1["seconds_solve"], "outer_iters": r1["solve"]["iters"],
                                                   "fell_back": r1["solve"]["fell_back"], "eta_rel_dev": dev(r1)},
                            adjoint_learned_mixed_at_bar={"tolerance": tol_b, "seconds": rb["seconds_solve"],
-                                                         "outer_iters": rb["solve"]["iters"], "eta_rel_dev": dev(rb)},
+                                                         "outer_iters": rb["solve"]["iters"], "eta_rel_dev": dev(rb),
+                                                         "eta_dev_over_bound": abs(rb["eta"] - rr["eta"]) /
+                                                         abs(rr["bound"])},
                            eta=rb["eta"], eta_reference=rr["eta"], bound=rb["bound"])
                 target = int(target_elems * growth ** (cycle - 1.0))  # src/main_nested.cpp:119-120
                 size = api.size_field(d, rb["base_error"], target)
@@ -795,7 +827,7 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
                           "Fp_old": m.get_state(api.FP_OLD), "eqps": m.get_state(api.EQPS),
                           "eqps_old": m.get_state(api.EQPS_OLD)}
             out.append(rec)
-            log("adaptive cycle: " + json.dumps({k: v for k, v in rec.items() if not isinstance(v, dict)}))
+            log("adaptive cycle: " + json.dumps(rec))
             del m, s, bcs, d
     return out
 
