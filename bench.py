@@ -430,9 +430,14 @@ def adjoint_arms(api, plain=True, learned_fp64=True):
 
 
 def _solve_record(r):
+    """One nested-adjoint run: the linear solve's seconds and counts, eta and
+    the bound; seconds_adjoint is the nested state transfer plus the ADJOINT
+    assembly and the boundary conditions, seconds_localize the error chain and
+    the indicators."""
     return {"seconds": r["seconds_solve"], "iters": r["solve"]["iters"], "inner_iters": r["solve"]["inner_iters"],
             "converged": r["solve"]["converged"], "fell_back": r["solve"]["fell_back"],
-            "rel_res": r["solve"]["rel_res"], "eta": r["eta"], "bound": r["bound"]}
+            "rel_res": r["solve"]["rel_res"], "eta": r["eta"], "bound": r["bound"],
+            "seconds_adjoint": r["seconds_adjoint"], "seconds_localize": r["seconds_localize"]}
 
 
 def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_check=True, goal_attempts=True,
@@ -496,8 +501,10 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
                                 "J_rel_dev_last": abs(newton["J"][-1] - Jr[-1]) / abs(Jr[-1])}
         del ref_p
     net, keep, train = train_learned(api)
+    t_n = time.perf_counter()
     na = api.NestedAdjoint(m, dbcs, [])
-    out.update(nested_elements=na.disc.num_elems, nested_dofs=na.disc.num_dofs, training=train)
+    out.update(nested_elements=na.disc.num_elems, nested_dofs=na.disc.num_dofs, training=train,
+               nested_create_seconds=time.perf_counter() - t_n, nested_disc_build=na.disc.build_times())
     net.attach(na.si_handle())
     t_now, t_old = float(steps), float(steps - 1)
 
@@ -726,7 +733,9 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
     for step in range(1, steps + 1):
         t_now, t_old = float(step), float(step - 1)
         for cycle in range(cycles + 1):
+            t_d = time.perf_counter()
             d = api.Disc(mesh)
+            t_disc = time.perf_counter() - t_d
 
             def start_mechanics():
                 mech = api.Mechanics(d, api.J2, mats)
@@ -773,13 +782,17 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
             rec = {"step": step, "cycle": cycle, "elements": mesh.num_elems, "dofs": d.num_dofs,
                    "newton_iters": newton["iters"], "newton_seconds": t_newton, "J": J,
                    **({"newton_retry": retry} if retry else {}),
+                   "disc_seconds": t_disc, "disc_build": d.build_times(),
                    "assembly_elem_per_s": mesh.num_elems / (ms * 1e-3), "assembly_ms": ms,
                    "assembly_hbm_gbs": alg / (ms * 1e-3) / 1e9}
             if cycle < cycles:
                 api.set_jac_dbcs(m, s, bcs, t_now)
                 net = api.Learned(seed=0)
                 net.train([s], epochs=60, lr=2e-3, num_probes=8)
+                t_n = time.perf_counter()
                 na = api.NestedAdjoint(m, dbcs, [])
+                rec["nested_create_seconds"] = time.perf_counter() - t_n
+                rec["nested_disc_build"] = na.disc.build_times()
                 lm = dict(precond=api.PRECOND_LEARNED, learned_cap=1500, **mix)
                 net.attach(na.si_handle())
                 if na.disc.num_dofs <= fp64_reference_max_dofs:

@@ -98,6 +98,14 @@ class Disc:
         check(lib().goal_disc_stream(self.h, ctypes.byref(p)))
         return int(p.value or 0)
 
+    def build_times(self) -> dict:
+        """Wall seconds of the build's phases and the colouring's round count."""
+        t = np.zeros(5)
+        rounds = ctypes.c_int()
+        check(lib().goal_disc_build_times(self.h, _ptr(t), ctypes.byref(rounds)))
+        return {"graph": float(t[0]), "colouring": float(t[1]), "layout": float(t[2]), "contribution_lists": float(t[3]),
+                "sets": float(t[4]), "colour_rounds": int(rounds.value)}
+
     def nested(self) -> "Disc":
         """Nested(d, UNIFORM): uniformly refined copy."""
         h = ctypes.c_void_p()

@@ -295,6 +295,14 @@ int goal_disc_sizes(goal_disc d, long long* sizes) {
   GOAL_API_END
 }
 
+int goal_disc_build_times(goal_disc d, double* seconds, int* color_rounds) {
+  GOAL_API_BEGIN
+  GOAL_ARG(d && seconds && color_rounds && d->d->built, "goal_disc_build_times: disc not built");
+  for (int k = 0; k < 5; ++k) seconds[k] = d->d->build_seconds[k];
+  *color_rounds = d->d->color_rounds;
+  GOAL_API_END
+}
+
 int goal_disc_get_graph(goal_disc d, int* row_ptr, int* col_idx) {
   GOAL_API_BEGIN
   GOAL_ARG(d && row_ptr && col_idx && d->d->built, "goal_disc_get_graph: disc not built");

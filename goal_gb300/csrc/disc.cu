@@ -11,6 +11,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <chrono>
 
 #include "disc.cuh"
 
@@ -288,6 +289,14 @@ void Disc::build() {
   GOAL_REQUIRE(num_nodes > 0 && num_elems > 0, GOAL_ERR_ARG, "empty mesh");
   cudaStream_t s = stream;
   const int N = num_nodes, E = num_elems;
+  auto clock = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+  double tp = clock();
+  auto phase = [&](int k) {  // closes phase k at a stream synchronisation
+    GOAL_CUDA(cudaStreamSynchronize(s));
+    const double t = clock();
+    build_seconds[k] = t - tp;
+    tp = t;
+  };
   coords.upload(coords_h.data(), coords_h.size(), s);
   DevBuf<int> tets_o, es_o;
   tets_o.upload(tets_h.data(), tets_h.size(), s);
@@ -338,6 +347,7 @@ void Disc::build() {
   offd.alloc(nnzb - N);
   k_offd<<<grid_for(N, 256), 256, 0, s>>>(N, brow_ptr.ptr, diag.ptr, offd.ptr);
   GOAL_CHECK_LAUNCH();
+  phase(0);
 
   // colouring
   DevBuf<int> ca, cb, rem, ovf;
@@ -365,6 +375,8 @@ void Disc::build() {
   GOAL_CUDA(cudaMemcpyAsync(&hovf, ovf.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
   GOAL_CUDA(cudaStreamSynchronize(s));
   GOAL_REQUIRE(hovf == 0, GOAL_ERR_CAPACITY, "element colouring needs more than 128 colours");
+  color_rounds = rounds;
+  phase(1);
 
   // colour-major order (stable in element id)
   DevBuf<int> ids, csorted, perm;
@@ -405,7 +417,7 @@ void Disc::build() {
                                               elem_pos.ptr, blk.ptr, first.ptr, color.ptr, grads.ptr, vol.ptr,
                                               h.ptr);
   GOAL_CHECK_LAUNCH();
-  GOAL_CUDA(cudaStreamSynchronize(s));
+  phase(2);
   {
     // contribution lists (stable sorts keep the element order within a block / node)
     DevBuf<int> bk, bv, nk, nv, bks, nks, bcnt, ncnt;
@@ -430,6 +442,7 @@ void Disc::build() {
     nks.alloc(4ll * E);
     nlist.alloc(4ll * E);
     sort_pairs(nk.ptr, nks.ptr, nv.ptr, nlist.ptr, 4 * E, bits_for(N), s);
+    phase(3);
   }
 
   // node sets / side sets to the device
@@ -456,7 +469,7 @@ void Disc::build() {
     ss.inc_ptr.upload(ptr.data(), ptr.size(), s);
     ss.inc.upload(inc.data(), inc.size(), s);
   }
-  GOAL_CUDA(cudaStreamSynchronize(s));
+  phase(4);
   built = true;
 }
 

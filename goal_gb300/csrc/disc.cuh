@@ -68,6 +68,11 @@ struct Disc {
   long long nnz = 0;     // scalar nonzeros (16 x nnzb)
   int nnzb = 0, num_colors = 0;
   std::vector<int> color_ptr;  // host copy
+  // wall seconds of build()'s phases: node graph (upload, incidence sort,
+  // block graph), colouring (Jones-Plassmann rounds), layout (colour-major
+  // order, block slots, geometry), contribution lists, node and side sets
+  double build_seconds[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  int color_rounds = 0;
   cudaStream_t stream = nullptr;
 
   // host copies of the input (original element order)

@@ -81,6 +81,13 @@ int goal_disc_add_side_set(goal_disc d, const char* name, int num_sides, const i
 int goal_disc_build_data(goal_disc d);
 /* sizes[0..5] = num_nodes, num_elems, num_dofs, nnz, nnzb (4x4 blocks), num_colors */
 int goal_disc_sizes(goal_disc d, long long* sizes);
+/* Wall seconds of the last build_data (Disc::compute_graphs and the element
+ * layout, src/goal_disc.cpp:195-222, 307-332), by phase: seconds[0] node graph
+ * (upload, node-element incidence sort, block graph), [1] element colouring
+ * (Jones-Plassmann rounds; *color_rounds of them), [2] element layout
+ * (colour-major order, block slots, geometry), [3] the sorted contribution
+ * lists of the two-phase assembly, [4] node and side sets. */
+int goal_disc_build_times(goal_disc d, double* seconds, int* color_rounds);
 /* The owned CSR graph of dRdu (Disc::compute_graphs, src/goal_disc.cpp:307-332):
  * row_ptr[num_dofs+1], col_idx[nnz], columns sorted. */
 int goal_disc_get_graph(goal_disc d, int* row_ptr, int* col_idx);

@@ -99,6 +99,11 @@ def test_coloring_is_valid(meshes, name):
     for c in range(d.num_colors):
         nodes = mesh.tets[col == c].ravel()
         assert len(np.unique(nodes)) == len(nodes), f"colour {c} shares nodes"
+    # the build's phase times: every phase ran, the colouring took at least
+    # one Jones-Plassmann round per colour beyond the first
+    bt = d.build_times()
+    assert all(bt[k] >= 0.0 for k in ("graph", "colouring", "layout", "contribution_lists", "sets"))
+    assert bt["colour_rounds"] >= d.num_colors
 
 
 @pytest.mark.parametrize("colored", [False, True])
