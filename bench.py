@@ -692,6 +692,15 @@ def learned_eval_leg(api, held_out, train_problems=8, train_target=20000, eval_t
 
 
 # ------------------------------------------------------------------ adaptive loop
+def _field_elements(mesh, vtx_size):
+    """The element count a size field asks for: sum over the elements of
+    (h_e / h_target)^3, h_e the rms edge length, h_target the mean of the
+    element's vertex sizes."""
+    x, t = mesh.coords, mesh.tets
+    h2 = sum(((x[t[:, a]] - x[t[:, b]]) ** 2).sum(axis=1) for a, b in ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)))
+    return float(((np.sqrt(h2 / 6.0) / vtx_size[t].mean(axis=1)) ** 3).sum())
+
+
 def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference_max_dofs=12_000_000):
     """The goal-oriented adaptive loop of GoalNested (src/main_nested.cpp:107-153)
     on the graded block of the learned-preconditioner study (seed 7: J2, 8
@@ -836,6 +845,7 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
                            eta=rb["eta"], eta_reference=rr["eta"], bound=rb["bound"])
                 target = int(target_elems * growth ** (cycle - 1.0))  # src/main_nested.cpp:119-120
                 size = api.size_field(d, rb["base_error"], target)
+                rec["field_elements"] = _field_elements(mesh, size)
                 na.close()
                 del na, net
                 U = m.get_solution().reshape(-1, 4)
