@@ -537,8 +537,8 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
     for name, prm in arms.items():
         tight = dict(out[name], tolerance=ADJ_TOL)
         for tol in (1e-11, 1e-12):
-            if tight["eta_rel_dev"] <= ETA_BAR:
-                break
+            if tight["eta_rel_dev"] <= ETA_BAR or not tight["converged"]:
+                break  # within the bar, or the arm's iteration cap already reached
             tight = run(f"{name}_{tol:g}", api.solve_params(**dict(prm, tolerance=tol)))
             tight["tolerance"] = tol
             tight["eta_rel_dev"] = abs(tight["eta"] - eta_ref) / abs(eta_ref)
@@ -701,7 +701,7 @@ def _field_elements(mesh, vtx_size):
     return float(((np.sqrt(h2 / 6.0) / vtx_size[t].mean(axis=1)) ** 3).sum())
 
 
-def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference_max_dofs=12_000_000):
+def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference_max_dofs=12_000_000, records=None):
     """The goal-oriented adaptive loop of GoalNested (src/main_nested.cpp:107-153)
     on the graded block of the learned-preconditioner study (seed 7: J2, 8
     material regions), KS von Mises (rho = 20), u_x = 0.04 t on x=4: for each
@@ -737,7 +737,7 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
     mix = dict(krylov_size=30, tolerance=1e-10, max_iters=3000, precision=api.MIXED, inner_iters=INNER_ITERS)
     target_elems = int(start * growth)
     U = states = None
-    out = []
+    out = [] if records is None else records
     fp64_tflops = None
     for step in range(1, steps + 1):
         t_now, t_old = float(step), float(step - 1)
@@ -870,6 +870,15 @@ def adaptive_leg(api, cycles, start, growth=2.0, seed=7, steps=1, fp64_reference
             log("adaptive cycle: " + json.dumps(rec))
             del m, s, bcs, d
     return out
+
+
+def adaptive_leg_partial(api, *args, **kwargs):
+    """adaptive_leg, with the cycles done so far kept when a cycle raises."""
+    done = []
+    try:
+        return adaptive_leg(api, *args, records=done, **kwargs)
+    except Exception as exc:  # the records of the finished cycles stand
+        return done + [{"error": str(exc)[:300]}]
 
 
 # ------------------------------------------------------------------ replicas
@@ -1061,8 +1070,8 @@ def main():
         legs.append(("adjoint_solve", lambda: adjoint_leg(a.adjoint_n, api, steps=a.adjoint_steps, qoi_check=False,
                                                           ramp=dict(jitter=0.0))))
     if a.adaptive_cycles > 0:
-        legs.append(("adaptive_loop", lambda: adaptive_leg(api, a.adaptive_cycles, a.adaptive_start,
-                                                           growth=a.adaptive_growth, steps=a.adaptive_steps)))
+        legs.append(("adaptive_loop", lambda: adaptive_leg_partial(api, a.adaptive_cycles, a.adaptive_start,
+                                                                   growth=a.adaptive_growth, steps=a.adaptive_steps)))
     if a.learned_eval > 0:
         if a.learned_scale == "full":
             legs.append(("learned_eval", lambda: learned_eval_leg(api, a.learned_eval, train_problems=34,
