@@ -504,60 +504,86 @@ __global__ void __launch_bounds__(128) k_elem(const ElemArgs a) {
   for (int b = 0; b < 4; ++b) twv[b] = a.stab ? tJV * wv[b] : 0.0;
   const double tJVs = a.stab ? tJV : 0.0;
   const unsigned fm = (!BUF && a.overwrite) ? __ldg(a.d.first + s) : 0u;
+  // ga V C G_a and Z_a = zs h_a
+  double CG[4][3], Zv[4][3];
 #pragma unroll
   for (int ai = 0; ai < 4; ++ai) {
-    double CG[3];  // ga V C G_a
     if constexpr (MODEL == MODEL_J2) {
-      CG[0] = gaV * (C[0] * G[ai][0] + C[3] * G[ai][1] + C[5] * G[ai][2]);
-      CG[1] = gaV * (C[3] * G[ai][0] + C[1] * G[ai][1] + C[4] * G[ai][2]);
-      CG[2] = gaV * (C[5] * G[ai][0] + C[4] * G[ai][1] + C[2] * G[ai][2]);
+      CG[ai][0] = gaV * (C[0] * G[ai][0] + C[3] * G[ai][1] + C[5] * G[ai][2]);
+      CG[ai][1] = gaV * (C[3] * G[ai][0] + C[1] * G[ai][1] + C[4] * G[ai][2]);
+      CG[ai][2] = gaV * (C[5] * G[ai][0] + C[4] * G[ai][1] + C[2] * G[ai][2]);
     } else {
-      CG[0] = gaV * G[ai][0]; CG[1] = gaV * G[ai][1]; CG[2] = gaV * G[ai][2];
+      CG[ai][0] = gaV * G[ai][0]; CG[ai][1] = gaV * G[ai][1]; CG[ai][2] = gaV * G[ai][2];
     }
-    const double Za0 = zs * hv[ai][0], Za1 = zs * hv[ai][1], Za2 = zs * hv[ai][2];
-    const double up0 = upf * hv[ai][0], up1 = upf * hv[ai][1], up2 = upf * hv[ai][2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) Zv[ai][k] = zs * hv[ai][k];
+  }
+  // Element block (ai, b) from Pc[i][k] = h_bi Z_ak + c_ab d_ik (TP: Pc
+  // transposed), written to the element buffer or accumulated into the matrix.
+  auto block = [&](int ai, int b, const double (&Pc)[3][3], bool TP, double eab) {
+    double K[4][4];
     const double pu1 = twv[ai] - pu0;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) K[i][k] = fma(hv[ai][i], Xp[b][k], fma(qv[ai][i], Yp[b][k], TP ? Pc[k][i] : Pc[i][k]));
+      K[i][3] = upf * hv[ai][i];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) K[3][k] = fma(pu1, hv[b][k], -fma(eab, tvv[k], twv[b] * hv[ai][k]));
+    K[3][3] = fma(tJVs, eab, ppc);
+    if constexpr (BUF) {
+      double* eb = a.ebuf + (size_t)(s - a.ebase) * a.estride + 16 + 16 * (4 * ai + b);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) st4(eb + 4 * r, K[r][0], K[r][1], K[r][2], K[r][3]);
+    } else if (MODE == MODE_PRIMAL) {
+      const int q = 4 * ai + b;
+      double* blk = a.A + 16ll * __ldg(a.d.blk + q * E + s);
+      const bool f1 = (fm >> q) & 1u;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc4(blk + 4 * r, f1, K[r][0], K[r][1], K[r][2], K[r][3]);
+    } else if (MODE == MODE_ADJOINT) {
+      const int q = 4 * b + ai;
+      double* blk = a.A + 16ll * __ldg(a.d.blk + q * E + s);
+      const bool f1 = (fm >> q) & 1u;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc4(blk + 4 * r, f1, K[0][r], K[1][r], K[2][r], K[3][r]);
+    }
+  };
+  // The off-diagonal blocks in pairs: c_ab and e_ab are symmetric in (a, b)
+  // and the term h_bi Z_ak = zs h_bi h_ak of block (a, b) is the term
+  // (k, i) of block (b, a), so each pair forms them once.
+#pragma unroll
+  for (int ai = 0; ai < 4; ++ai) {
+#pragma unroll
+    for (int b = ai + 1; b < 4; ++b) {
       const double eab = hv[ai][0] * hv[b][0] + hv[ai][1] * hv[b][1] + hv[ai][2] * hv[b][2];
-      if constexpr (DSUM) {
-        if (ai == b) {  // resolved at compile time (both loops unrolled)
-          st4(a.ebuf + (size_t)(s - a.ebase) * a.estride + 16 + 16 * (4 * ai + b), up0, up1, up2, fma(tJVs, eab, ppc));
-          continue;
-        }
-      }
-      const double cab = fma(CG[0], G[b][0], fma(CG[1], G[b][1], CG[2] * G[b][2]));
-      double K[4][4];
+      const double cab = fma(CG[ai][0], G[b][0], fma(CG[ai][1], G[b][1], CG[ai][2] * G[b][2]));
+      double Pc[3][3];
 #pragma unroll
-      for (int i = 0; i < 3; ++i) {
+      for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const double Zak = (k == 0) ? Za0 : ((k == 1) ? Za1 : Za2);
-          const double t0 = (i == k) ? fma(hv[b][i], Zak, cab) : hv[b][i] * Zak;
-          K[i][k] = fma(hv[ai][i], Xp[b][k], fma(qv[ai][i], Yp[b][k], t0));
-        }
-        K[i][3] = (i == 0) ? up0 : ((i == 1) ? up1 : up2);
-      }
+        for (int k = 0; k < 3; ++k) Pc[i][k] = (i == k) ? fma(hv[b][i], Zv[ai][k], cab) : hv[b][i] * Zv[ai][k];
+      block(ai, b, Pc, false, eab);
+      block(b, ai, Pc, true, eab);
+    }
+  }
+  // the diagonal blocks (a, a)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) K[3][k] = fma(pu1, hv[b][k], -fma(eab, tvv[k], twv[b] * hv[ai][k]));
-      K[3][3] = fma(tJVs, eab, ppc);
-      if constexpr (BUF) {
-        double* eb = a.ebuf + (size_t)(s - a.ebase) * a.estride + 16 + 16 * (4 * ai + b);
+  for (int ai = 0; ai < 4; ++ai) {
+    const double eaa = hv[ai][0] * hv[ai][0] + hv[ai][1] * hv[ai][1] + hv[ai][2] * hv[ai][2];
+    if constexpr (DSUM) {
+      // column 3 only: the u columns come from the row sums in the gather
+      st4(a.ebuf + (size_t)(s - a.ebase) * a.estride + 16 + 16 * (5 * ai), upf * hv[ai][0], upf * hv[ai][1],
+          upf * hv[ai][2], fma(tJVs, eaa, ppc));
+    } else {
+      const double caa = fma(CG[ai][0], G[ai][0], fma(CG[ai][1], G[ai][1], CG[ai][2] * G[ai][2]));
+      double Pc[3][3];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) st4(eb + 4 * r, K[r][0], K[r][1], K[r][2], K[r][3]);
-      } else if (MODE == MODE_PRIMAL) {
-        const int q = 4 * ai + b;
-        double* blk = a.A + 16ll * __ldg(a.d.blk + q * E + s);
-        const bool f1 = (fm >> q) & 1u;
+      for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int r = 0; r < 4; ++r) acc4(blk + 4 * r, f1, K[r][0], K[r][1], K[r][2], K[r][3]);
-      } else if (MODE == MODE_ADJOINT) {
-        const int q = 4 * b + ai;
-        double* blk = a.A + 16ll * __ldg(a.d.blk + q * E + s);
-        const bool f1 = (fm >> q) & 1u;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) acc4(blk + 4 * r, f1, K[0][r], K[1][r], K[2][r], K[3][r]);
-      }
+        for (int k = 0; k < 3; ++k) Pc[i][k] = (i == k) ? fma(hv[ai][i], Zv[ai][k], caa) : hv[ai][i] * Zv[ai][k];
+      block(ai, ai, Pc, false, eaa);
     }
   }
   }  // JAC
