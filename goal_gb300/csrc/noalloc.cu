@@ -124,8 +124,7 @@ extern "C" int goal_avg_disp_noalloc(const double* coords, const int* tets, cons
   double* scratch = nullptr;
   {
     // First call on a device, with that device current: look up the scratch
-    // array's address once. This runs before the launches below, so it must
-    // not happen while a stream is being captured.
+    // array's address once (a runtime query, made before the launches below).
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (g_scratch[dev] == nullptr) {
       void* p = nullptr;

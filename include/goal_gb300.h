@@ -445,8 +445,8 @@ int goal_learned_destroy(goal_learned l);
  * that must not pay for an allocation. The partial sums live in a fixed 128 KiB device array of this
  * library, which limits a call to 16,777,216 elements (GOAL_ERR_CAPACITY
  * beyond). The first call on each device, with that device current, looks up
- * that array's address; make it before any stream capture. Nothing has to be
- * zeroed beforehand; *J is overwritten. Calls that overlap in time share the
+ * that array's address. Nothing has to be zeroed beforehand; *J is
+ * overwritten. Calls that overlap in time share the
  * array and race: issue them on one stream or order them with events. A node
  * id outside [0, num_nodes) makes *J NaN. Same value as goal_assemble with
  * GOAL_NONE and GOAL_QOI_AVG_DISP up to summation order. */
