@@ -302,7 +302,7 @@ def run_reference(a):
 # write stops.
 LOAD_INC = 0.002    # u_x increment per load step (yield strain Y/E = 0.00125)
 RAMP_STEPS = 10     # u_x = 0.02 at the last step
-# FP32 inner iterations per outer step of the nested adjoint solves: the inner
+# inner iterations per outer step of the nested adjoint solves: the inner
 # iterations (one Gram-Schmidt pass, binary16 matrix) are cheaper than outer
 # ones, so a longer inner solve wins (40^3 nested adjoint, learned + mixed:
 # 0.72 s with 30, 0.60 s with 45, 0.59 s with 60)
@@ -319,7 +319,7 @@ def _j2_ramp(api, n, steps, seed=1, max_newton=12, precision=None, lin_tol=1e-10
     LOAD_INC t on x=1 at t = 1, 2, ...), the states updated between steps, on a
     Kuhn cube with jittered interior nodes (no grid symmetry), with goal's
     Newton (src/goal_primal.cpp:111-137). ``precision`` selects the linear
-    solver of the Newton steps (default: FP32-inner / FP64-outer); ``qoi``
+    solver of the Newton steps (default: binary16-inner / FP64-outer); ``qoi``
     records the KS von Mises functional after every step; ``fp_reset`` the J2
     state write at elastic points (True: Fp = Fp_old; False: goal's).
 

@@ -95,7 +95,7 @@ def test_training_and_gain_over_block_jacobi():
     assert plain["converged"] and learned["converged"]
     assert learned["iters"] < 0.8 * plain["iters"]
     assert np.linalg.norm(x1 - x0) <= 1e-7 * np.linalg.norm(x0)
-    # the learned two-sweep inside the FP32-inner / FP64-outer solve: the same
+    # the learned two-sweep inside the binary16-inner / FP64-outer solve: the same
     # solution, fewer outer iterations than plain block-Jacobi in that solver,
     # and bitwise repeatable (fixed reduction orders, no atomics)
     pm = dict(prm, krylov_size=30, precision=api.MIXED, inner_iters=30)

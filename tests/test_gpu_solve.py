@@ -3,7 +3,8 @@ oracle (calls through the C ABI).
 
 * linear solve: true relative residual <= 1e-10 (the stopping rule), and the
   solution within 1e-8 relative of a direct solve of the oracle's matrix;
-  FP64 and mixed (FP32 inner / FP64 outer) modes give the same answer.
+  FP64 and mixed (binary16-stored inner in FP32 arithmetic / FP64 outer)
+  modes give the same answer.
 * Newton on the reference's own 3D regression cases: the final QoI within the
   reference's tolerance (1e-8) of its stored value, and the same Newton
   iteration counts as the oracle.
