@@ -51,3 +51,98 @@ def test_adaptive_leg_keeps_finished_cycles(monkeypatch):
 def test_adaptive_leg_partial_passes_results_through(monkeypatch):
     monkeypatch.setattr(bench, "adaptive_leg", lambda api, *a, records=None, **kw: [{"cycle": 0}])
     assert bench.adaptive_leg_partial(None, 1, 10) == [{"cycle": 0}]
+
+
+class _FakeApi:
+    """Stands in for goal_gb300.api in bench._j2_ramp: a Newton solve fails
+    when its load increment exceeds ``max_inc``; calls are recorded."""
+
+    J2 = MIXED = NONE = QOI_KS_VM = 0
+
+    class GoalError(RuntimeError):
+        pass
+
+    def __init__(self, max_inc):
+        self.max_inc = max_inc
+        self.calls = []
+        api = self
+
+        class Mechanics:
+            def __init__(self, d, model, mats, fp_reset=False):
+                self.U = np.zeros(4)
+                self.updates = 0
+
+            def set_line_search(self, k):
+                pass
+
+            def update_states(self):
+                self.updates += 1
+                api.calls.append(("update",))
+
+            def get_solution(self):
+                return self.U.copy()
+
+            def set_solution(self, U):
+                self.U = np.asarray(U, dtype=float).copy()
+                api.calls.append(("restore", float(self.U[0])))
+
+        self.Mechanics = Mechanics
+        self.Disc = lambda mesh: object()
+        self.SolInfo = lambda d: object()
+        self.Bcs = lambda d, dbcs, tbcs: object()
+
+    @staticmethod
+    def solve_params(**kw):
+        return kw
+
+    def primal_solve(self, m, s, bcs, t_now, t_old, max_iters, tol, prm):
+        self.calls.append(("solve", t_old, t_now))
+        if t_now - t_old > self.max_inc + 1e-12:
+            m.U[:] = -1.0  # a diverged iterate
+            e = self.GoalError("newton failed")
+            e.stats = {"norms": [1.0] * max_iters}
+            raise e
+        m.U[:] = t_now
+        return {"iters": 3, "linear_iters": 30, "backtracks": 0}
+
+    def assemble(self, *a, **kw):
+        return 0.0
+
+
+def test_ramp_cutbacks_halve_failed_increments_and_grow_back():
+    api = _FakeApi(max_inc=0.5)
+    *_, out = bench._j2_ramp(api, 2, 3, max_newton=12, cutbacks=6, jitter=0.0)
+    # step 1: 1.0 fails, then 0.5 + 0.5; step 2: 0.5 x 2; the fourth success
+    # in a row (the end of step 2) lets step 3 try a full step, which fails,
+    # and step 3 ends in halves
+    solves = [c[1:] for c in api.calls if c[0] == "solve"]
+    assert solves[0] == (0.0, 1.0)
+    assert (0.0, 0.5) in solves and (0.5, 1.0) in solves
+    assert out["substeps"] == [2, 2, 2]
+    # Newton iterations per load step: the failed attempt's 12 plus 3 per substep
+    assert out["iters"][0] == 12 + 2 * 3
+    # a failed attempt restores the solution it started from
+    restores = [c[1] for c in api.calls if c[0] == "restore"]
+    assert restores and all(r >= 0.0 for r in restores)
+    # the states are updated once before every solve that follows a success
+    seq = [c[0] for c in api.calls]
+    for i, c in enumerate(seq):
+        if c == "update":
+            assert seq[i + 1] == "solve"
+
+
+def test_ramp_without_cutbacks_is_goals_newton():
+    api = _FakeApi(max_inc=0.5)
+    with pytest.raises(_FakeApi.GoalError) as exc:
+        bench._j2_ramp(api, 2, 3, cutbacks=0, jitter=0.0)
+    assert exc.value.step == 1
+    assert [c[0] for c in api.calls] == ["solve"]
+
+
+def test_ramp_gives_up_after_its_cutbacks():
+    api = _FakeApi(max_inc=0.1)
+    with pytest.raises(_FakeApi.GoalError) as exc:
+        bench._j2_ramp(api, 2, 2, cutbacks=2, jitter=0.0)
+    assert exc.value.step == 1
+    incs = [c[2] - c[1] for c in api.calls if c[0] == "solve"]
+    assert incs == [1.0, 0.5, 0.25]
