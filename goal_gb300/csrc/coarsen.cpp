@@ -144,8 +144,13 @@ struct Coarsener {
     thread_local std::vector<uint64_t> elab, ea, eb;
     adjacent(b, adj_b);
     if (!std::binary_search(adj_b.begin(), adj_b.end(), a)) return false;
-    // geometry: the tets that keep b (as a) stay valid and good enough; no
-    // new edge too long
+    // no new edge too long (checked first: it needs no tet quality)
+    for (int c : adj_b) {
+      if (c == a) continue;
+      const double s = refine_ratio * 0.5 * (size[a] + size[c]);
+      if (len2(a, c) > s * s) return false;
+    }
+    // geometry: the tets that keep b (as a) stay valid and good enough
     double worst = 1.0;
     for (int t : vt[b])
       if (talive[t]) worst = std::min(worst, quality(T[t]));
@@ -156,11 +161,6 @@ struct Coarsener {
       for (int& x : v)
         if (x == b) x = a;
       if (!(vol6(v) > 0.0) || quality(v) < qmin) return false;
-    }
-    for (int c : adj_b) {
-      if (c == a) continue;
-      const double s = refine_ratio * 0.5 * (size[a] + size[c]);
-      if (len2(a, c) > s * s) return false;
     }
     // link condition: the vertices adjacent to both a and b are exactly the
     // vertices of the tets around edge ab; edges (c, d) seen from both a and b
@@ -586,21 +586,24 @@ struct Coarsener {
       uint64_t key;
     };
     std::vector<Cand> cand;
-    std::vector<uint64_t> keys;
-    keys.reserve(6 * T.size());
-    for (size_t t = 0; t < T.size(); ++t) {
-      if (!talive[t]) continue;
-      const auto& v = T[t];
-      for (int i = 0; i < 4; ++i)
-        for (int j = i + 1; j < 4; ++j) keys.push_back(ekey(v[i], v[j]));
-    }
-    std::sort(keys.begin(), keys.end());
-    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-    for (uint64_t k : keys) {
-      const int lo = (int)(k & 0xffffffffu), hi = (int)(k >> 32);
-      const double s = 0.5 * (size[lo] + size[hi]);
-      const double r = std::sqrt(len2(lo, hi)) / s;
-      if (r < ratio) cand.push_back({r, k});
+    // every edge once, from its lower end point: the higher neighbours of v
+    // in v's live tets (a local sort per vertex instead of one of all edges)
+    std::vector<int> nb;
+    for (int lo = 0; lo < N; ++lo) {
+      if (!valive[lo]) continue;
+      nb.clear();
+      for (int t : vt[lo]) {
+        if (!talive[t]) continue;
+        for (int x : T[t])
+          if (x > lo) nb.push_back(x);
+      }
+      std::sort(nb.begin(), nb.end());
+      nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+      for (int hi : nb) {
+        const double s = 0.5 * (size[lo] + size[hi]);
+        const double r = std::sqrt(len2(lo, hi)) / s;
+        if (r < ratio) cand.push_back({r, ekey(lo, hi)});
+      }
     }
     std::sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) {
       return x.r != y.r ? x.r < y.r : x.key < y.key;
