@@ -46,6 +46,10 @@ struct Coarsener {
   std::vector<int> eset;
   std::vector<int> origin;  // original element of each tet (swaps make new ones)
   std::vector<char> talive;
+  // quality of every live tet at the start of a coarsening pass: a collapse
+  // changes only tets whose vertices it marks touched, so the tets around an
+  // untouched vertex keep these values for the rest of the pass
+  std::vector<double> tq;
   std::vector<std::vector<int>> vt;  // vertex -> tets (live ones; dead entries are filtered on use)
   // boundary faces (faces of exactly one tet) and side triangles
   std::vector<std::array<int, 3>> F;
@@ -153,7 +157,7 @@ struct Coarsener {
     // geometry: the tets that keep b (as a) stay valid and good enough
     double worst = 1.0;
     for (int t : vt[b])
-      if (talive[t]) worst = std::min(worst, quality(T[t]));
+      if (talive[t]) worst = std::min(worst, tq[t]);
     const double qmin = std::min(min_quality, worst);
     for (int t : vt[b]) {
       if (!talive[t] || has(T[t], a)) continue;
@@ -608,6 +612,9 @@ struct Coarsener {
     std::sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) {
       return x.r != y.r ? x.r < y.r : x.key < y.key;
     });
+    tq.assign(T.size(), 0.0);
+    for (size_t t = 0; t < T.size(); ++t)
+      if (talive[t]) tq[t] = quality(T[t]);
     std::vector<char> touched(N, 0);
     std::vector<int> adj;
     int done = 0;
