@@ -54,6 +54,8 @@ def _args():
     ap.add_argument("--precision-n", type=int, default=0,
                     help="base mesh of the precision leg (64: the 64^3 cube of the precision configuration; 0: skip)")
     ap.add_argument("--precision-steps", type=int, default=10, help="load steps of the precision leg's ramp")
+    ap.add_argument("--precision-plain-cap", type=int, default=150000,
+                    help="iteration limit of the precision leg's plain FP64 arm")
     ap.add_argument("--learned-eval", type=int, default=20,
                     help="held-out seeds of the learned-preconditioner study (0: skip)")
     ap.add_argument("--learned-scale", choices=["small", "full"], default="small",
@@ -406,7 +408,7 @@ def train_learned(api, epochs=60):
                        "loss_first": float(losses[0]), "loss_last": float(losses[-1])}
 
 
-def adjoint_arms(api, plain=True, learned_fp64=True):
+def adjoint_arms(api, plain=True, learned_fp64=True, plain_cap=45000):
     """The solver arms of the adjoint comparison, all to ADJ_TOL: plain FP64
     block-Jacobi FGMRES(100) (the baseline), the learned correction in FP64,
     the nested FGMRES(30) solves with 60 inner iterations in FP64, FP32 and
@@ -417,7 +419,7 @@ def adjoint_arms(api, plain=True, learned_fp64=True):
     lrn = dict(precond=api.PRECOND_LEARNED, learned_cap=500)
     arms = {}
     if plain:
-        arms["plain_fp64"] = dict(krylov_size=100, tolerance=ADJ_TOL, max_iters=45000)
+        arms["plain_fp64"] = dict(krylov_size=100, tolerance=ADJ_TOL, max_iters=plain_cap)
     if learned_fp64:
         arms["learned_fp64"] = dict(krylov_size=100, tolerance=ADJ_TOL, max_iters=30000,
                                     precond=api.PRECOND_LEARNED, learned_cap=15000)
@@ -441,7 +443,7 @@ def _solve_record(r):
 
 
 def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_check=True, goal_attempts=True,
-                ramp=None):
+                ramp=None, plain_cap=45000):
     """Adjoint solve on the nested (uniformly refined) mesh after the J2 load
     ramp of the stretched cube (u_x = LOAD_INC t on x=1, t = 1..steps; u=0 on
     x=0): dRdu^T z = dM/du with the KS von Mises functional (rho = 20), the
@@ -461,7 +463,8 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
     max 15 iterations) with goal's J2 state write and with the Fp_old reset,
     and reports the step where each stops converging.
     ``ramp``: the globalization of the load ramp (_j2_ramp's jitter,
-    line_search, cutbacks, max_newton)."""
+    line_search, cutbacks, max_newton). ``plain_cap``: the plain FP64 arm's
+    iteration limit."""
     import torch
     ramp = dict(ramp or {})
     jit = ramp.get("jitter", JITTER)
@@ -526,7 +529,7 @@ def adjoint_leg(n, api, steps=RAMP_STEPS, plain=True, learned_fp64=True, qoi_che
     out["reference"] = dict(ref, solver=f"nested FGMRES(30), {INNER_ITERS} FP64 inner iterations, FP64 storage")
     out["reference"]["check_eta_rel_dev"] = abs(chk["eta"] - eta_ref) / abs(eta_ref)
     out["reference"]["check_solver"] = "learned + binary16 nested FGMRES to the same tolerance"
-    arms = adjoint_arms(api, plain, learned_fp64)
+    arms = adjoint_arms(api, plain, learned_fp64, plain_cap)
     for name, prm in arms.items():
         rec = run(name, api.solve_params(**prm))
         rec["eta_rel_dev"] = abs(rec["eta"] - eta_ref) / abs(eta_ref)
@@ -1081,11 +1084,13 @@ def main():
         else:
             legs.append(("learned_eval", lambda: learned_eval_leg(api, a.learned_eval)))
     if a.precision_n > 0:
-        # jittered 64^3 cube: full Newton fails at the first step there, backtracking converges every step
+        # jittered 64^3 cube: full Newton fails at the first step there, backtracking converges every step;
+        # plain FP64 block-Jacobi needs more than 45,000 iterations on its nested adjoint
         legs.append(("precision_64", lambda: adjoint_leg(a.precision_n, api, steps=a.precision_steps,
                                                          learned_fp64=False, goal_attempts=False,
                                                          ramp=dict(jitter=JITTER, line_search=8, max_newton=30,
-                                                                   lin_max_iters=3000))))
+                                                                   lin_max_iters=3000),
+                                                         plain_cap=a.precision_plain_cap)))
     t_legs = time.perf_counter()
     for name, fn in legs:
         if time.perf_counter() - t_legs > a.leg_budget:
