@@ -285,22 +285,31 @@ int tuned_assemble(int N, int E, const int* tets, const int* elem_set, const dou
           Yp[b][k] = V * (-(2.0 / 3.0) * ga * hv[b][k] + alpha * (yq * qv[b][k] + yh * hv[b][k] + yn * nv[b][k]));
         }
       const double zs = V * (ga * Ic3 - pJ);
+      // C G_b once per node; c_ab = ga V G_a.C G_b and e_ab = h_a.h_b are
+      // symmetric in (a, b), and the term zs h_br h_ak of block (a, b) is the
+      // term (k, r) of block (b, a): the blocks are formed in pairs
+      double CGv[4][3];
+      for (int b = 0; b < 4; ++b)
+        for (int r = 0; r < 3; ++r) CGv[b][r] = Cm[r][0] * G[b][0] + Cm[r][1] * G[b][1] + Cm[r][2] * G[b][2];
+      auto block = [&](int a, int b, const double (&P)[3][3], bool tp, double eab) {
+        double* K = A + 16ll * blk[16ll * e + 4 * a + b];
+        for (int r = 0; r < 3; ++r) {
+          for (int k = 0; k < 3; ++k) K[4 * r + k] += hv[a][r] * Xp[b][k] + qv[a][r] * Yp[b][k] + (tp ? P[k][r] : P[r][k]);
+          K[4 * r + 3] += V * J * hv[a][r] * 0.25;
+        }
+        for (int k = 0; k < 3; ++k)
+          K[12 + k] += V * (hv[b][k] * (tauJ * wv[a] - (J + Jinv) * 0.125) - tauJ * eab * vv[k] - tauJ * wv[b] * hv[a][k]);
+        K[15] += V * (1.0 / (16.0 * kappa) + tauJ * eab);
+      };
       for (int a = 0; a < 4; ++a)
-        for (int b = 0; b < 4; ++b) {
-          double CG = 0.0;
-          for (int r = 0; r < 3; ++r)
-            CG += G[a][r] * (Cm[r][0] * G[b][0] + Cm[r][1] * G[b][1] + Cm[r][2] * G[b][2]);
-          const double cab = ga * V * CG;
+        for (int b = a; b < 4; ++b) {
+          const double cab = ga * V * (G[a][0] * CGv[b][0] + G[a][1] * CGv[b][1] + G[a][2] * CGv[b][2]);
           const double eab = hv[a][0] * hv[b][0] + hv[a][1] * hv[b][1] + hv[a][2] * hv[b][2];
-          double* K = A + 16ll * blk[16ll * e + 4 * a + b];
-          for (int r = 0; r < 3; ++r) {
-            for (int k = 0; k < 3; ++k)
-              K[4 * r + k] += hv[a][r] * Xp[b][k] + qv[a][r] * Yp[b][k] + zs * hv[b][r] * hv[a][k] + (r == k ? cab : 0.0);
-            K[4 * r + 3] += V * J * hv[a][r] * 0.25;
-          }
-          for (int k = 0; k < 3; ++k)
-            K[12 + k] += V * (hv[b][k] * (tauJ * wv[a] - (J + Jinv) * 0.125) - tauJ * eab * vv[k] - tauJ * wv[b] * hv[a][k]);
-          K[15] += V * (1.0 / (16.0 * kappa) + tauJ * eab);
+          double P[3][3];
+          for (int r = 0; r < 3; ++r)
+            for (int k = 0; k < 3; ++k) P[r][k] = zs * hv[b][r] * hv[a][k] + (r == k ? cab : 0.0);
+          block(a, b, P, false, eab);
+          if (b != a) block(b, a, P, true, eab);
         }
     }
   }
