@@ -669,12 +669,6 @@ int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, co
     // boundary faces: the faces of exactly one tet (sorted vertex triples,
     // sorted, counted by runs)
     static const int kFaces[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
-    struct FaceRec {
-      std::array<int, 3> key;  // sorted vertices
-      std::array<int, 3> v;    // as in the tet
-    };
-    std::vector<FaceRec> all;
-    all.reserve(4ull * num_elems);
     for (int e = 0; e < num_elems; ++e) {
       for (int q = 0; q < 4; ++q) {
         const int v = tets[4ll * e + q];
@@ -684,21 +678,52 @@ int goal_coarsener_create(int num_nodes, const double* coords, int num_elems, co
       }
       c.eset[e] = elem_set ? elem_set[e] : 0;
       c.origin.push_back(e);
-      for (auto& fq : kFaces) {
-        FaceRec r;
-        r.v = {c.T[e][fq[0]], c.T[e][fq[1]], c.T[e][fq[2]]};
-        r.key = r.v;
-        std::sort(r.key.begin(), r.key.end());
-        all.push_back(r);
-      }
     }
-    std::sort(all.begin(), all.end(), [](const FaceRec& x, const FaceRec& y) { return x.key < y.key; });
+    // faces grouped by their smallest vertex (a counting sort over the
+    // nodes), then matched within each group by the other two vertices
+    struct FaceRec {
+      uint64_t rest;  // (middle << 32) | largest vertex
+      int tet, q;
+    };
+    std::vector<long long> start(num_nodes + 1, 0);
+    auto face_key = [&](int e, int q, int& lo, uint64_t& rest) {
+      int k[3] = {c.T[e][kFaces[q][0]], c.T[e][kFaces[q][1]], c.T[e][kFaces[q][2]]};
+      std::sort(k, k + 3);
+      lo = k[0];
+      rest = ((uint64_t)(unsigned)k[1] << 32) | (uint64_t)(unsigned)k[2];
+    };
+    for (int e = 0; e < num_elems; ++e)
+      for (int q = 0; q < 4; ++q) {
+        int lo;
+        uint64_t rest;
+        face_key(e, q, lo, rest);
+        ++start[lo + 1];
+      }
+    for (int n = 0; n < num_nodes; ++n) start[n + 1] += start[n];
+    std::vector<FaceRec> all(4ull * num_elems);
+    {
+      std::vector<long long> fill(start.begin(), start.end() - 1);
+      for (int e = 0; e < num_elems; ++e)
+        for (int q = 0; q < 4; ++q) {
+          int lo;
+          uint64_t rest;
+          face_key(e, q, lo, rest);
+          all[fill[lo]++] = {rest, e, q};
+        }
+    }
     std::vector<std::array<int, 3>> bfaces;
-    for (size_t i = 0; i < all.size();) {
-      size_t j = i + 1;
-      while (j < all.size() && all[j].key == all[i].key) ++j;
-      if (j - i == 1) bfaces.push_back(all[i].v);
-      i = j;
+    for (int n = 0; n < num_nodes; ++n) {
+      auto b0 = all.begin() + start[n], b1 = all.begin() + start[n + 1];
+      std::sort(b0, b1, [](const FaceRec& x, const FaceRec& y) { return x.rest < y.rest; });
+      for (auto i = b0; i != b1;) {
+        auto j = i + 1;
+        while (j != b1 && j->rest == i->rest) ++j;
+        if (j - i == 1) {
+          const auto& fq = kFaces[i->q];
+          bfaces.push_back({c.T[i->tet][fq[0]], c.T[i->tet][fq[1]], c.T[i->tet][fq[2]]});
+        }
+        i = j;
+      }
     }
     std::sort(bfaces.begin(), bfaces.end());  // deterministic order
     for (const auto& f : bfaces) {
